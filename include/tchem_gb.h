@@ -1,0 +1,134 @@
+/*
+ * C ABI of the GB300 engine for TChem-atm's batched box-model gas-chemistry time advance.
+ *
+ * Every entry point takes plain pointers and sizes. Device pointers are CUDA device
+ * addresses; `stream` is a cudaStream_t passed as void* (NULL = the legacy default stream).
+ * Calls that take device pointers are stream-ordered and asynchronous, like the Kokkos
+ * launch they replace; the caller synchronises. Return value: TCHEM_GB_OK or an error code,
+ * with a message available from tchem_gb_last_error() (thread-local).
+ *
+ * Reference interfaces replaced (paths inside the TChem-atm source tree):
+ *   tchem_gb_mech_create_*      TChem::KineticModelData(yamlFile) + createNCAR_KineticModelConstData
+ *                               src/core/TChem_KineticModelData.cpp:57-78,
+ *                               src/core/TChem_KineticModelNCAR_ConstData.hpp:115-148
+ *   tchem_gb_scenario_read      TChem::AtmChemistry::setScenarioConditions
+ *                               src/core/TChem_AtmosphericChemistry.cpp:430-508
+ *   tchem_gb_workspace_bytes    TChem::AtmosphericChemistry::getWorkSpaceSize
+ *                               src/core/TChem_AtmosphericChemistry.hpp:47-81
+ *   tchem_gb_time_advance       TChem::AtmosphericChemistry::runDeviceBatch (both overloads)
+ *                               src/core/TChem_AtmosphericChemistry.hpp:83-155,
+ *                               src/core/TChem_AtmosphericChemistry.cpp:211-271, 343-385
+ *   tchem_gb_kforward           TChem::Impl::KForwardAerosol::team_invoke
+ *                               src/core/impl/TChem_Impl_KForwardAerosol.hpp:44-145
+ *   tchem_gb_reaction_rates     TChem::Impl::ReactionRatesAerosol::team_invoke (box-model RHS)
+ *                               src/core/impl/TChem_Impl_ReactionRatesAerosol.hpp:57-143, 238-289
+ *   tchem_gb_jacobian           AtmosphericChemistry_Problem::computeJacobian (analytic here)
+ *                               src/core/problems/TChem_Impl_AtmosphericChemistry_Problem.hpp:202-213
+ */
+#ifndef TCHEM_GB_H
+#define TCHEM_GB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TCHEM_GB_ABI_VERSION 1
+
+enum tchem_gb_error {
+  TCHEM_GB_OK = 0,
+  TCHEM_GB_ERR_ARG = 1,         /* invalid argument (TCHEM_CHECK_ERROR in the reference) */
+  TCHEM_GB_ERR_PARSE = 2,       /* mechanism / scenario file could not be read */
+  TCHEM_GB_ERR_CUDA = 3,        /* a CUDA runtime call failed */
+  TCHEM_GB_ERR_UNSUPPORTED = 4, /* feature outside the box-model path (e.g. JPL rate types) */
+  TCHEM_GB_ERR_NOMEM = 5,       /* device allocation failed */
+  TCHEM_GB_ERR_DEVICE = 6       /* a device-side bounded wait or check reported an error */
+};
+
+/* Per-sample status written by the time advance. The reference signals a failed sample with
+ * dt_out < 0 (src/core/problems/TChem_Impl_AtmosphericChemistry.hpp:213-221); these codes
+ * refine it. Failed samples also follow the reference convention state_out = 0 for the
+ * active species, t_out = t_end, dt_out = -1. */
+enum tchem_gb_sample_status {
+  TCHEM_GB_SAMPLE_OK = 0,
+  TCHEM_GB_SAMPLE_NEWTON_FAIL = 1, /* Newton failed on 4 successive step halvings */
+  TCHEM_GB_SAMPLE_SKIPPED = 2,     /* t_out >= t_end on entry: nothing done */
+  TCHEM_GB_SAMPLE_NEGATIVE_DT = 3, /* dt_in < 0: returned without touching the outputs */
+  TCHEM_GB_SAMPLE_NONFINITE = 4,   /* non-finite value in the state or a step */
+  TCHEM_GB_SAMPLE_DT_UNDERFLOW = 5 /* step size reached 0 before t_end */
+};
+
+/* Mirrors TChem::TimeAdvance (src/core/TChem_Util.hpp:469-477), same field order and types. */
+typedef struct tchem_gb_time_advance {
+  double tbeg, tend;
+  double dt, dtmin, dtmax;
+  int32_t max_num_newton_iterations;
+  int32_t num_time_iterations_per_interval;
+  int32_t num_outer_time_iterations_per_interval;
+  int32_t jacobian_interval;
+} tchem_gb_time_advance;
+
+/* Host view of a parsed mechanism in the reference's table layout
+ * (TChem::KineticModelNCAR_ConstData, src/core/TChem_KineticModelNCAR_ConstData.hpp:30-113).
+ * All pointers are owned by the mechanism and valid until tchem_gb_mech_destroy. */
+typedef struct tchem_gb_kmcd_view {
+  int32_t nSpec, nConstSpec, nReac, maxSpecInReac, M_index;
+  double CONV_PPM;
+  const int32_t* reacNreac;    /* [nReac] */
+  const int32_t* reacNprod;    /* [nReac] */
+  const int32_t* reacSidx;     /* [nReac][maxSpecInReac] */
+  const double* reacNuki;      /* [nReac][maxSpecInReac] */
+  const int32_t* convExponent; /* [nReac] */
+  const int32_t* reacType;     /* [nReac]: 0 ARRHENIUS 1 TROE 2 CMAQ_H2O2 3 JPL 4 R_JPL_ARRHENIUS 5 PHOTO_RATE */
+  int32_t nArrhenius;
+  const int32_t* arrhenius_reaction; /* [nArrhenius] */
+  const double* arrhenius_param;     /* [nArrhenius][5]: E, A, B, C, D */
+  int32_t nTroe;
+  const int32_t* reacPfal;           /* [nTroe] */
+  const double* reacPpar;            /* [nTroe][8]: k0_A*1e6, k0_B, k0_C, kinf_A, kinf_B, kinf_C, Fc, N */
+  int32_t nCMAQ_H2O2;
+  const int32_t* cmaq_reaction;      /* [nCMAQ_H2O2] */
+  const double* cmaq_param;          /* [nCMAQ_H2O2][6]: A1, B1, C1, A2 (k2_A*1e6), B2, C2 */
+  int32_t nEmission;
+  const int32_t* emission_species;   /* [nEmission] */
+  const double* emission_rate;       /* [nEmission] */
+} tchem_gb_kmcd_view;
+
+/* Per-sample work counters of one time-advance call (the algorithmic-work inputs of the
+ * roofline: flops = n_lu*(2/3)m^3 + n_solve*2m^2 + n_jac*F_jac + n_rhs*F_rhs). */
+typedef struct tchem_gb_sample_stats {
+  int32_t n_steps;       /* accepted steps */
+  int32_t n_rejected;    /* step attempts rejected by the error test */
+  int32_t n_newton_fail; /* step attempts abandoned because Newton did not converge */
+  int32_t n_newton_iter; /* Newton iterations, both stages */
+  int32_t n_lu;          /* LU factorizations */
+  int32_t n_solve;       /* forward+backward solve pairs (Newton updates and error filter) */
+  int32_t n_rhs;         /* right-hand-side evaluations */
+  int32_t n_jac;         /* Jacobian evaluations */
+} tchem_gb_sample_stats;
+
+typedef struct tchem_gb_mech tchem_gb_mech; /* opaque */
+
+const char* tchem_gb_last_error(void);
+int tchem_gb_abi_version(void);
+
+/* Parses an NCAR-format YAML file. When echo_path is non-NULL the mechanism echo
+ * (the reference's kmod.echo format) is written there. */
+int tchem_gb_mech_create_from_file(const char* yaml_path, const char* echo_path, tchem_gb_mech** out);
+int tchem_gb_mech_create_from_string(const char* yaml_text, tchem_gb_mech** out);
+void tchem_gb_mech_destroy(tchem_gb_mech* mech);
+int tchem_gb_mech_host_view(const tchem_gb_mech* mech, tchem_gb_kmcd_view* view);
+/* Copies species name i (truncated as the reference stores it) into buf. */
+int tchem_gb_mech_species_name(const tchem_gb_mech* mech, int i, char* buf, int buflen);
+
+/* Scenario file -> state[nbatch][nSpec+3] on the host ([rho, p, T, x...]). */
+int tchem_gb_scenario_batch_size(const char* yaml_path, int* nbatch);
+int tchem_gb_scenario_read(const char* yaml_path, const tchem_gb_mech* mech, double* state_host, int nbatch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TCHEM_GB_H */

@@ -1,0 +1,6 @@
+"""CPU oracle for the batched TR-BDF2 box-model time advance (test infrastructure only).
+
+Only the tests, the smoke check and bench.py's CPU-baseline leg use this package; the engine
+never does.
+"""
+from .binding import Oracle, load  # noqa: F401

@@ -1,0 +1,97 @@
+"""ctypes binding of liboracle.so (test infrastructure only)."""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .build import LIB_PATH, build
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            build()
+        L = C.CDLL(str(LIB_PATH))
+        vp = C.c_void_p
+        L.oracle_kforward.restype = C.c_int
+        L.oracle_kforward.argtypes = [vp, C.c_double, C.c_double, vp]
+        L.oracle_reaction_rates.restype = C.c_int
+        L.oracle_reaction_rates.argtypes = [vp, C.c_double, C.c_double, vp, vp]
+        L.oracle_jacobian.restype = C.c_int
+        L.oracle_jacobian.argtypes = [vp, C.c_double, C.c_double, vp, vp]
+        L.oracle_time_advance.restype = C.c_int
+        L.oracle_time_advance.argtypes = [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                          C.c_int, C.c_int]
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray | None) -> C.c_void_p:
+    return C.c_void_p(0) if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """FP64 CPU restatement of the box-model path for one or more kinetic models.
+
+    ``models`` are objects with a ``view`` attribute (a KmcdView ctypes struct) that stay alive
+    for the lifetime of this object.
+    """
+
+    def __init__(self, models):
+        self.models = list(models)
+        self.lib = load()
+        self._views = [m.view for m in self.models]
+        self._ptrs = (C.c_void_p * len(self._views))(*[C.cast(C.pointer(v), C.c_void_p) for v in self._views])
+
+    def _vp(self, k: int = 0) -> C.c_void_p:
+        return C.cast(C.pointer(self._views[k]), C.c_void_p)
+
+    def kforward(self, T: float, p: float, k: int = 0) -> np.ndarray:
+        out = np.zeros(self.models[k].nReac)
+        assert self.lib.oracle_kforward(self._vp(k), T, p, _p(out)) == 0
+        return out
+
+    def reaction_rates(self, T: float, p: float, x: np.ndarray, k: int = 0) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.zeros(self.models[k].nSpec - self.models[k].nConstSpec)
+        assert self.lib.oracle_reaction_rates(self._vp(k), T, p, _p(x), _p(out)) == 0
+        return out
+
+    def jacobian(self, T: float, p: float, x: np.ndarray, k: int = 0) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        m = self.models[k].nSpec - self.models[k].nConstSpec
+        out = np.zeros((m, m))
+        assert self.lib.oracle_jacobian(self._vp(k), T, p, _p(x), _p(out)) == 0
+        return out
+
+    def time_advance(self, tadv: np.ndarray, state: np.ndarray, tol_newton, tol_time: np.ndarray,
+                     t_out: np.ndarray | None = None, mech_of_sample: np.ndarray | None = None,
+                     lu_fp32: bool = False, nthreads: int = 0):
+        """Returns (state_out, t_out, dt_out, status, stats)."""
+        B = state.shape[0]
+        state = np.ascontiguousarray(state, dtype=np.float64)
+        state_out = state.copy()
+        t_out = np.array(tadv["tbeg"], dtype=np.float64) if t_out is None else np.array(t_out, dtype=np.float64)
+        dt_out = np.zeros(B)
+        status = np.zeros(B, dtype=np.int32)
+        from tchem_gb._capi import SAMPLE_STATS_DTYPE  # struct layout shared with the engine
+        stats = np.zeros(B, dtype=SAMPLE_STATS_DTYPE)
+        tn = np.ascontiguousarray(tol_newton, dtype=np.float64)
+        tt = np.ascontiguousarray(tol_time, dtype=np.float64)
+        mos = None if mech_of_sample is None else np.ascontiguousarray(mech_of_sample, dtype=np.int32)
+        tadv = np.ascontiguousarray(tadv)
+        rc = self.lib.oracle_time_advance(self._ptrs, len(self._views), _p(mos), B, _p(tn), _p(tt), _p(tadv),
+                                          _p(state), _p(t_out), _p(dt_out), _p(state_out), _p(status), _p(stats),
+                                          int(lu_fp32), int(nthreads))
+        if rc != 0:
+            raise RuntimeError(f"oracle_time_advance returned {rc}")
+        return state_out, t_out, dt_out, status, stats
+
+
+def library_path() -> Path:
+    return LIB_PATH

@@ -1,0 +1,396 @@
+// CPU oracle: FP64 restatement of the reference's box-model RHS and a TR-BDF2 integrator.
+// TEST INFRASTRUCTURE ONLY (see oracle.h for scope and citations).
+#include "oracle.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+// --- rate constants: src/core/impl/TChem_Impl_KForwardAerosol.hpp:44-145 -----------------
+void kforward(const tchem_gb_kmcd_view& km, double t, double p, double* kfor) {
+  const double t_1 = 1.0 / t;
+  const double one = 1.0;
+  const double conv = km.CONV_PPM * p * t_1;
+  for (int r = 0; r < km.nReac; ++r) kfor[r] = 0.0;  // types outside the box path stay 0
+  for (int i = 0; i < km.nArrhenius; ++i) {
+    const double* P = km.arrhenius_param + 5 * i;
+    const double E = P[0], A = P[1], B = P[2], C = P[3], D = P[4];
+    const int r = km.arrhenius_reaction[i];
+    kfor[r] = A * std::exp(C * t_1) * (B == 0.0 ? one : std::pow(t / D, B)) * (E == 0.0 ? one : (one + E * p)) *
+              std::pow(conv, static_cast<double>(km.convExponent[r]));
+  }
+  for (int i = 0; i < km.nTroe; ++i) {
+    const double* rp = km.reacPpar + 8 * i;
+    const int r = km.reacPfal[i];
+    const double k0_A = rp[0], k0_B = rp[1], k0_C = rp[2];
+    const double kinf_A = rp[3], kinf_B = rp[4], kinf_C = rp[5], Fc = rp[6], N = rp[7];
+    const double k0 = k0_A * (k0_C == 0.0 ? one : std::exp(k0_C * t_1)) *
+                      (k0_B == 0.0 ? one : std::pow(t / 300.0, k0_B)) * conv;
+    const double k0_kinf = k0 / (kinf_A * (kinf_C == 0.0 ? one : std::exp(kinf_C * t_1)) *
+                                 (kinf_B == 0.0 ? one : std::pow(t / 300.0, kinf_B)));
+    kfor[r] = k0 / (1.0 + k0_kinf) * std::pow(Fc, 1.0 / (1.0 + std::pow(std::log10(k0_kinf) / N, 2.0))) *
+              std::pow(conv, static_cast<double>(km.convExponent[r]));
+  }
+  for (int i = 0; i < km.nCMAQ_H2O2; ++i) {
+    const double* P = km.cmaq_param + 6 * i;
+    const double A1 = P[0], B1 = P[1], C1 = P[2], A2 = P[3], B2 = P[4], C2 = P[5];
+    const int r = km.cmaq_reaction[i];
+    kfor[r] = (A1 * std::exp(C1 * t_1) * (B1 == 0.0 ? one : std::pow(t / 300.0, B1)) +
+               A2 * std::exp(C2 * t_1) * (B2 == 0.0 ? one : std::pow(t / 300.0, B2)) * conv) *
+              std::pow(conv, static_cast<double>(km.convExponent[r]));
+  }
+}
+
+// --- RHS: src/core/impl/TChem_Impl_ReactionRatesAerosol.hpp:57-143 --------------------------
+// concX[nSpec] (constant species last), kfor precomputed; omega[m].
+void reaction_rates(const tchem_gb_kmcd_view& km, const double* kfor, const double* concX, double* omega,
+                    double* rop) {
+  const int m = km.nSpec - km.nConstSpec;
+  const int S = km.maxSpecInReac;
+  for (int i = 0; i < m; ++i) omega[i] = 0.0;
+  for (int i = 0; i < km.nEmission; ++i) {
+    const int k = km.emission_species[i];
+    if (k < m) omega[k] = km.emission_rate[i];
+  }
+  for (int r = 0; r < km.nReac; ++r) {
+    double q = kfor[r];
+    for (int j = 0; j < km.reacNreac[r]; ++j) {
+      const int ks = km.reacSidx[r * S + j];
+      const int niup = std::abs(static_cast<int>(km.reacNuki[r * S + j]));
+      q *= std::pow(concX[ks], static_cast<double>(niup));
+    }
+    rop[r] = q;
+  }
+  const int joff = S / 2;
+  for (int r = 0; r < km.nReac; ++r) {
+    const double q = rop[r];
+    for (int j = 0; j < km.reacNreac[r]; ++j) {
+      const int ks = km.reacSidx[r * S + j];
+      if (ks < m) omega[ks] += km.reacNuki[r * S + j] * q;
+    }
+    for (int j = 0; j < km.reacNprod[r]; ++j) {
+      const int ks = km.reacSidx[r * S + j + joff];
+      if (ks < m) omega[ks] += km.reacNuki[r * S + j + joff] * q;
+    }
+  }
+}
+
+// --- analytic Jacobian of reaction_rates with respect to the active species ---------------
+void jacobian(const tchem_gb_kmcd_view& km, const double* kfor, const double* concX, double* J) {
+  const int m = km.nSpec - km.nConstSpec;
+  const int S = km.maxSpecInReac;
+  const int joff = S / 2;
+  std::fill(J, J + static_cast<size_t>(m) * m, 0.0);
+  for (int r = 0; r < km.nReac; ++r) {
+    const int nr = km.reacNreac[r];
+    for (int j = 0; j < nr; ++j) {
+      const int sj = km.reacSidx[r * S + j];
+      if (sj >= m) continue;
+      const int nj = std::abs(static_cast<int>(km.reacNuki[r * S + j]));
+      double dq = kfor[r] * nj * std::pow(concX[sj], static_cast<double>(nj - 1));
+      for (int l = 0; l < nr; ++l) {
+        if (l == j) continue;
+        const int sl = km.reacSidx[r * S + l];
+        const int nl = std::abs(static_cast<int>(km.reacNuki[r * S + l]));
+        dq *= std::pow(concX[sl], static_cast<double>(nl));
+      }
+      for (int k = 0; k < nr; ++k) {
+        const int sk = km.reacSidx[r * S + k];
+        if (sk < m) J[static_cast<size_t>(sk) * m + sj] += km.reacNuki[r * S + k] * dq;
+      }
+      for (int k = 0; k < km.reacNprod[r]; ++k) {
+        const int sk = km.reacSidx[r * S + k + joff];
+        if (sk < m) J[static_cast<size_t>(sk) * m + sj] += km.reacNuki[r * S + k + joff] * dq;
+      }
+    }
+  }
+}
+
+// --- dense LU with partial pivoting (row swaps; first maximum in the current row order) ---
+template <typename T>
+struct DenseLU {
+  int n = 0;
+  std::vector<T> a;
+  std::vector<int> piv;
+  std::vector<T> w;
+  void resize(int n_) {
+    n = n_;
+    a.assign(static_cast<size_t>(n) * n, T(0));
+    piv.assign(n, 0);
+    w.assign(n, T(0));
+  }
+  // A = I - c J, built in double and rounded to T.
+  bool factor(const double* J, double c) {
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        a[static_cast<size_t>(i) * n + j] = static_cast<T>((i == j ? 1.0 : 0.0) - c * J[static_cast<size_t>(i) * n + j]);
+    for (int k = 0; k < n; ++k) {
+      int p = k;
+      T amax = std::abs(a[static_cast<size_t>(k) * n + k]);
+      for (int i = k + 1; i < n; ++i) {
+        const T v = std::abs(a[static_cast<size_t>(i) * n + k]);
+        if (v > amax) { amax = v; p = i; }
+      }
+      if (!(amax > T(0)) || !std::isfinite(static_cast<double>(amax))) return false;
+      piv[k] = p;
+      if (p != k)
+        for (int j = 0; j < n; ++j) std::swap(a[static_cast<size_t>(k) * n + j], a[static_cast<size_t>(p) * n + j]);
+      const T inv = T(1) / a[static_cast<size_t>(k) * n + k];
+      for (int i = k + 1; i < n; ++i) {
+        const T l = a[static_cast<size_t>(i) * n + k] * inv;
+        a[static_cast<size_t>(i) * n + k] = l;
+        for (int j = k + 1; j < n; ++j) a[static_cast<size_t>(i) * n + j] -= l * a[static_cast<size_t>(k) * n + j];
+      }
+    }
+    return true;
+  }
+  // x = A^{-1} b (b and x in double, arithmetic in T).
+  void solve(const double* b, double* x) {
+    for (int i = 0; i < n; ++i) w[i] = static_cast<T>(b[i]);
+    for (int k = 0; k < n; ++k)
+      if (piv[k] != k) std::swap(w[k], w[piv[k]]);
+    for (int k = 0; k < n; ++k) {
+      const T wk = w[k];
+      for (int i = k + 1; i < n; ++i) w[i] -= a[static_cast<size_t>(i) * n + k] * wk;
+    }
+    for (int k = n - 1; k >= 0; --k) {
+      T s = w[k];
+      for (int j = k + 1; j < n; ++j) s -= a[static_cast<size_t>(k) * n + j] * w[j];
+      w[k] = s / a[static_cast<size_t>(k) * n + k];
+    }
+    for (int i = 0; i < n; ++i) x[i] = static_cast<double>(w[i]);
+  }
+};
+
+struct Settings {
+  int max_newton, jac_interval, max_iters;
+  double atol_newton, rtol_newton;
+  const double* tol_time;  // [m][2]
+};
+
+// One sample: RHS/Jacobian closure over the fixed T, p and constant concentrations.
+template <typename LU_T>
+struct Sample {
+  const tchem_gb_kmcd_view& km;
+  int m, n;
+  std::vector<double> kfor, rop, concX, J;
+  DenseLU<LU_T> lu;
+  tchem_gb_sample_stats st{};
+
+  Sample(const tchem_gb_kmcd_view& km_, double T, double p, const double* xconst)
+      : km(km_), m(km_.nSpec - km_.nConstSpec), n(km_.nSpec) {
+    kfor.assign(km.nReac, 0.0);
+    rop.assign(km.nReac, 0.0);
+    concX.assign(n, 0.0);
+    J.assign(static_cast<size_t>(m) * m, 0.0);
+    for (int i = 0; i < n - m; ++i) concX[m + i] = xconst[i];
+    kforward(km, T, p, kfor.data());
+    lu.resize(m);
+  }
+  void f(const double* y, double* out) {
+    std::copy(y, y + m, concX.begin());
+    reaction_rates(km, kfor.data(), concX.data(), out, rop.data());
+    ++st.n_rhs;
+  }
+  void jac(const double* y) {
+    std::copy(y, y + m, concX.begin());
+    jacobian(km, kfor.data(), concX.data(), J.data());
+    ++st.n_jac;
+  }
+
+  // Solves y - c f(y) = rhs by Newton from the guess in y.
+  bool newton(double* y, const double* rhs, double c, const Settings& s, std::vector<double>& fy,
+              std::vector<double>& g, std::vector<double>& dx) {
+    for (int it = 0; it < s.max_newton; ++it) {
+      f(y, fy.data());
+      for (int i = 0; i < m; ++i) g[i] = -((y[i] - c * fy[i]) - rhs[i]);
+      if (it % s.jac_interval == 0) {
+        jac(y);
+        if (!lu.factor(J.data(), c)) return false;
+        ++st.n_lu;
+      }
+      lu.solve(g.data(), dx.data());
+      ++st.n_solve;
+      ++st.n_newton_iter;
+      double sdx = 0.0, sy = 0.0;
+      for (int i = 0; i < m; ++i) {
+        y[i] += dx[i];
+        sdx += dx[i] * dx[i];
+        sy += y[i] * y[i];
+      }
+      const double ndx = std::sqrt(sdx), ny = std::sqrt(sy);
+      if (!std::isfinite(ndx) || !std::isfinite(ny)) return false;
+      if (ndx <= s.atol_newton + s.rtol_newton * ny) return true;
+    }
+    return false;
+  }
+
+  int integrate(double* y, double t_beg, double t_end, double dt_in, double dt_min, double dt_max, const Settings& s,
+                double& t_out, double& dt_out) {
+    if (dt_in < 0.0) return TCHEM_GB_SAMPLE_NEGATIVE_DT;
+    const double gamma = 2.0 - std::sqrt(2.0);
+    const double d = 0.5 * gamma;                                  // diagonal coefficient of both stages
+    const double cg = 1.0 / (gamma * (2.0 - gamma));               // BDF2 stage: weight of y_gamma
+    const double cn = (1.0 - gamma) * (1.0 - gamma) / (gamma * (2.0 - gamma));  // and of y_n
+    const double kappa = (-3.0 * gamma * gamma + 4.0 * gamma - 2.0) / (12.0 * (2.0 - gamma));
+    const double e0 = 1.0 / gamma, e1 = -1.0 / (gamma * (1.0 - gamma)), e2 = 1.0 / (1.0 - gamma);
+
+    std::vector<double> fn(m), fg(m), f1(m), yg(m), y1(m), rhs(m), fy(m), g(m), dx(m), est(m), estf(m);
+    double t = t_beg, dt = dt_in;
+    int status = TCHEM_GB_SAMPLE_OK;
+    f(y, fn.data());
+    for (int iter = 0; iter < s.max_iters && t < t_end; ++iter) {
+      bool converged = false, last = false;
+      for (int ntry = 0; ntry < 4; ++ntry) {
+        dt = std::min(std::max(dt, dt_min), dt_max);
+        last = dt >= t_end - t;
+        if (last) dt = t_end - t;
+        if (!(dt > 0.0)) { status = TCHEM_GB_SAMPLE_DT_UNDERFLOW; break; }
+        const double c = d * dt;
+        // stage 1 (trapezoidal rule to t + gamma dt)
+        for (int i = 0; i < m; ++i) { rhs[i] = y[i] + c * fn[i]; yg[i] = y[i]; }
+        bool ok = newton(yg.data(), rhs.data(), c, s, fy, g, dx);
+        if (ok) {
+          // stage 2 (BDF2 through t, t + gamma dt, t + dt)
+          f(yg.data(), fg.data());
+          for (int i = 0; i < m; ++i) { rhs[i] = cg * yg[i] - cn * y[i]; y1[i] = yg[i]; }
+          ok = newton(y1.data(), rhs.data(), c, s, fy, g, dx);
+        }
+        if (ok) { converged = true; break; }
+        ++st.n_newton_fail;
+        dt *= 0.5;
+      }
+      if (status != TCHEM_GB_SAMPLE_OK) break;
+      if (!converged) { status = TCHEM_GB_SAMPLE_NEWTON_FAIL; break; }
+      f(y1.data(), f1.data());
+      // local error estimate, filtered through (I - d dt J)^{-1}
+      for (int i = 0; i < m; ++i) est[i] = 2.0 * kappa * dt * (e0 * fn[i] + e1 * fg[i] + e2 * f1[i]);
+      lu.solve(est.data(), estf.data());
+      ++st.n_solve;
+      double err = 0.0;
+      for (int i = 0; i < m; ++i) {
+        const double w = s.tol_time[2 * i] + s.tol_time[2 * i + 1] * std::max(std::abs(y[i]), std::abs(y1[i]));
+        err = std::max(err, std::abs(estf[i]) / w);
+      }
+      if (!std::isfinite(err)) { status = TCHEM_GB_SAMPLE_NONFINITE; break; }
+      if (err <= 1.0 || dt <= dt_min) {
+        t = last ? t_end : t + dt;
+        std::copy(y1.begin(), y1.end(), y);
+        fn.swap(f1);
+        ++st.n_steps;
+        double fac = err > 0.0 ? 0.9 * std::cbrt(1.0 / err) : 2.0;
+        fac = std::max(0.2, std::min(2.0, fac));
+        dt = std::min(dt * fac, dt_max);
+        if (t + dt > t_end) dt = t_end - t;
+      } else {
+        ++st.n_rejected;
+        dt *= std::max(0.2, 0.9 * std::cbrt(1.0 / err));
+      }
+    }
+    t_out = t;
+    dt_out = dt;
+    if (status != TCHEM_GB_SAMPLE_OK) {
+      for (int i = 0; i < m; ++i) y[i] = 0.0;
+      t_out = t_end;
+      dt_out = -1.0;
+    }
+    return status;
+  }
+};
+
+template <typename LU_T>
+void run_batch(const tchem_gb_kmcd_view* const* kms, const int32_t* mech_of_sample, int nbatch, const double* tol_newton,
+               const double* tol_time, const tchem_gb_time_advance* tadv, const double* state, double* t_out,
+               double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats) {
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int b = 0; b < nbatch; ++b) {
+    const tchem_gb_kmcd_view& km = *kms[mech_of_sample ? mech_of_sample[b] : 0];
+    const int n = km.nSpec, m = km.nSpec - km.nConstSpec, dim = n + 3;
+    const tchem_gb_time_advance& ta = tadv[b];
+    tchem_gb_sample_stats st0{};
+    if (stats) stats[b] = st0;
+    if (t_out[b] >= ta.tend) {
+      if (status) status[b] = TCHEM_GB_SAMPLE_SKIPPED;
+      continue;
+    }
+    const double* row = state + static_cast<size_t>(b) * dim;
+    double* out = state_out + static_cast<size_t>(b) * dim;
+    const double rho = row[0], p = row[1], T = row[2];
+    std::vector<double> y(row + 3, row + 3 + m);
+    std::vector<double> xconst(row + 3 + m, row + 3 + n);
+    Sample<LU_T> smp(km, T, p, xconst.data());
+    Settings s{ta.max_num_newton_iterations, std::max(1, ta.jacobian_interval), ta.num_time_iterations_per_interval,
+               tol_newton[0], tol_newton[1], tol_time};
+    double to = 0.0, dto = 0.0;
+    const int st = smp.integrate(y.data(), ta.tbeg, ta.tend, ta.dt, ta.dtmin, ta.dtmax, s, to, dto);
+    if (status) status[b] = st;
+    if (stats) stats[b] = smp.st;
+    if (st == TCHEM_GB_SAMPLE_NEGATIVE_DT) continue;  // outputs untouched
+    out[0] = rho;
+    out[1] = p;
+    out[2] = T;
+    for (int i = 0; i < m; ++i) out[3 + i] = y[i];
+    for (int i = 0; i < n - m; ++i) out[3 + m + i] = xconst[i];
+    t_out[b] = to;
+    dt_out[b] = dto;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int oracle_kforward(const tchem_gb_kmcd_view* km, double T, double p, double* kfor) {
+  if (!km || !kfor) return TCHEM_GB_ERR_ARG;
+  kforward(*km, T, p, kfor);
+  return TCHEM_GB_OK;
+}
+
+int oracle_reaction_rates(const tchem_gb_kmcd_view* km, double T, double p, const double* x, double* omega) {
+  if (!km || !x || !omega) return TCHEM_GB_ERR_ARG;
+  std::vector<double> kfor(km->nReac), rop(km->nReac);
+  kforward(*km, T, p, kfor.data());
+  reaction_rates(*km, kfor.data(), x, omega, rop.data());
+  return TCHEM_GB_OK;
+}
+
+int oracle_jacobian(const tchem_gb_kmcd_view* km, double T, double p, const double* x, double* J) {
+  if (!km || !x || !J) return TCHEM_GB_ERR_ARG;
+  std::vector<double> kfor(km->nReac);
+  kforward(*km, T, p, kfor.data());
+  jacobian(*km, kfor.data(), x, J);
+  return TCHEM_GB_OK;
+}
+
+int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                        const double* tol_newton, const double* tol_time, const tchem_gb_time_advance* tadv,
+                        const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
+                        tchem_gb_sample_stats* stats, int lu_fp32, int nthreads) {
+  if (!kms || n_mechs <= 0 || nbatch < 0 || !tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out ||
+      !state_out)
+    return TCHEM_GB_ERR_ARG;
+  if (mech_of_sample)
+    for (int b = 0; b < nbatch; ++b)
+      if (mech_of_sample[b] < 0 || mech_of_sample[b] >= n_mechs) return TCHEM_GB_ERR_ARG;
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  if (lu_fp32)
+    run_batch<float>(kms, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status, stats);
+  else
+    run_batch<double>(kms, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status, stats);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(prev);
+#endif
+  return TCHEM_GB_OK;
+}
+
+}  // extern "C"

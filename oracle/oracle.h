@@ -1,0 +1,58 @@
+/*
+ * CPU oracle for the batched box-model TR-BDF2 time advance.
+ *
+ * TEST INFRASTRUCTURE ONLY. This library is the checker for the GPU engine: it is loaded by
+ * the tests, by the smoke check and by the CPU-baseline leg of bench.py, and by nothing on
+ * the product path. It is a plain FP64 C++ restatement of the reference algorithm:
+ *   rate constants   src/core/impl/TChem_Impl_KForwardAerosol.hpp:44-145
+ *   RHS              src/core/impl/TChem_Impl_ReactionRatesAerosol.hpp:57-143, 238-289
+ *   problem          src/core/problems/TChem_Impl_AtmosphericChemistry_Problem.hpp:64-81, 127-143
+ *   batch driver     src/core/TChem_AtmosphericChemistry.cpp:42-167 (skip samples at t_end,
+ *                    T, p, rho copied through)
+ *   integrator       TR-BDF2 of Bank et al. (IEEE Trans. Electron Devices 32(10), 1985) with the
+ *                    error estimate of Hosea & Shampine (Appl. Numer. Math. 20, 1996). The
+ *                    reference's integrator (Tines TimeIntegratorTrBDF2) is an external
+ *                    dependency absent from the source tree; the restatement keeps its call
+ *                    interface (src/core/problems/TChem_Impl_AtmosphericChemistry.hpp:138-155)
+ *                    and the behaviour the reference's own outputs pin: dt doubles per accepted
+ *                    step while the error is negligible, is capped by dt_max, the last step lands
+ *                    exactly on t_end and dt_out is 0 there
+ *                    (src/unit-tests/CB05CL_AE5/references/full_gas.hdf5,
+ *                    src/examples/runs/atmospheric_chemistry/Emission/Emissions.dat); Newton
+ *                    failure halves dt up to 4 times, then the sample fails with state 0,
+ *                    t_out = t_end, dt_out = -1 (src/core/impl/TChem_Impl_TimeIntegratorImplicitEuler.hpp:246-305).
+ * The Jacobian is analytic (the reference uses forward differences or Sacado AD; both give
+ * the same matrix to rounding, and the Newton fixed point does not depend on it).
+ */
+#ifndef TCHEM_GB_ORACLE_H
+#define TCHEM_GB_ORACLE_H
+
+#include "../include/tchem_gb.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* kfor[nReac] for one (T, p). */
+int oracle_kforward(const tchem_gb_kmcd_view* km, double T, double p, double* kfor);
+/* omega[m] = d x_active / dt for x[nSpec] (constant species last). */
+int oracle_reaction_rates(const tchem_gb_kmcd_view* km, double T, double p, const double* x, double* omega);
+/* J[m][m] = d omega_i / d x_j (row-major), analytic. */
+int oracle_jacobian(const tchem_gb_kmcd_view* km, double T, double p, const double* x, double* J);
+
+/* Batched time advance with the reference's runDeviceBatch semantics on host arrays.
+ * kms[n_mechs] with mech_of_sample[nbatch] (NULL: every sample uses kms[0]).
+ * lu_fp32 = 0: FP64 Newton LU (the plain form); 1: FP32 LU and solves with FP64 residuals
+ * (the algorithm of the engine's mixed-precision form, for like-for-like checks).
+ * t_out is read (samples with t_out >= tend are skipped) and written.
+ * nthreads <= 0 uses all OpenMP threads. stats may be NULL. */
+int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                        const double* tol_newton, const double* tol_time, const tchem_gb_time_advance* tadv,
+                        const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
+                        tchem_gb_sample_stats* stats, int lu_fp32, int nthreads);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,189 @@
+// C ABI: mechanism and scenario entry points (host only).
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+
+#include "mech_host.hpp"
+
+namespace tchem_gb {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_last_error(const std::string& msg) { g_last_error = msg; }
+
+void destroy_device_tables(DeviceTables* t);  // defined with the device code
+
+}  // namespace tchem_gb
+
+using tchem_gb::set_last_error;
+
+void tchem_gb_mech::build_view() {
+  const auto& k = km;
+  arrhenius_reaction.clear();
+  arrhenius_param.clear();
+  for (const auto& a : k.arrhenius) {
+    arrhenius_reaction.push_back(a.reaction_index);
+    const double p[5] = {a.E, a.A, a.B, a.C, a.D};
+    arrhenius_param.insert(arrhenius_param.end(), p, p + 5);
+  }
+  cmaq_reaction.clear();
+  cmaq_param.clear();
+  for (const auto& c : k.cmaq_h2o2) {
+    cmaq_reaction.push_back(c.reaction_index);
+    const double p[6] = {c.A1, c.B1, c.C1, c.A2, c.B2, c.C2};
+    cmaq_param.insert(cmaq_param.end(), p, p + 6);
+  }
+  emission_species.clear();
+  emission_rate.clear();
+  for (const auto& e : k.emission) {
+    emission_species.push_back(e.species_index);
+    emission_rate.push_back(e.emission_rate);
+  }
+  reacPfal.assign(k.reacPfal.begin(), k.reacPfal.end());
+
+  view.nSpec = k.nSpec;
+  view.nConstSpec = k.nConstSpec;
+  view.nReac = k.nReac;
+  view.maxSpecInReac = k.maxSpecInReac;
+  view.M_index = k.M_index;
+  view.CONV_PPM = k.CONV_PPM_;
+  view.reacNreac = k.reacNreac.data();
+  view.reacNprod = k.reacNprod.data();
+  view.reacSidx = k.reacSidx.data();
+  view.reacNuki = k.reacNuki.data();
+  view.convExponent = k.convExponent.data();
+  view.reacType = k.reacType.data();
+  view.nArrhenius = static_cast<int32_t>(arrhenius_reaction.size());
+  view.arrhenius_reaction = arrhenius_reaction.data();
+  view.arrhenius_param = arrhenius_param.data();
+  view.nTroe = static_cast<int32_t>(reacPfal.size());
+  view.reacPfal = reacPfal.data();
+  view.reacPpar = k.reacPpar.data();
+  view.nCMAQ_H2O2 = static_cast<int32_t>(cmaq_reaction.size());
+  view.cmaq_reaction = cmaq_reaction.data();
+  view.cmaq_param = cmaq_param.data();
+  view.nEmission = static_cast<int32_t>(emission_species.size());
+  view.emission_species = emission_species.data();
+  view.emission_rate = emission_rate.data();
+}
+
+tchem_gb_mech::~tchem_gb_mech() {
+  for (auto* t : device_tables)
+    if (t) tchem_gb::destroy_device_tables(t);
+}
+
+extern "C" {
+
+const char* tchem_gb_last_error(void) { return tchem_gb::g_last_error.c_str(); }
+
+int tchem_gb_abi_version(void) { return TCHEM_GB_ABI_VERSION; }
+
+int tchem_gb_mech_create_from_file(const char* yaml_path, const char* echo_path, tchem_gb_mech** out) {
+  if (!yaml_path || !out) {
+    set_last_error("tchem_gb_mech_create_from_file: null argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  *out = nullptr;
+  try {
+    std::unique_ptr<tchem_gb_mech> m(new tchem_gb_mech());
+    if (echo_path) {
+      std::ofstream echo(echo_path);
+      if (!echo) throw std::runtime_error(std::string("cannot open echo file ") + echo_path);
+      m->km = tchem_gb::KineticModel::fromYamlFile(yaml_path, &echo);
+    } else {
+      m->km = tchem_gb::KineticModel::fromYamlFile(yaml_path, nullptr);
+    }
+    m->build_view();
+    *out = m.release();
+    return TCHEM_GB_OK;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return TCHEM_GB_ERR_PARSE;
+  }
+}
+
+int tchem_gb_mech_create_from_string(const char* yaml_text, tchem_gb_mech** out) {
+  if (!yaml_text || !out) {
+    set_last_error("tchem_gb_mech_create_from_string: null argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  *out = nullptr;
+  try {
+    std::unique_ptr<tchem_gb_mech> m(new tchem_gb_mech());
+    m->km = tchem_gb::KineticModel::fromYamlString(yaml_text, nullptr);
+    m->build_view();
+    *out = m.release();
+    return TCHEM_GB_OK;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return TCHEM_GB_ERR_PARSE;
+  }
+}
+
+void tchem_gb_mech_destroy(tchem_gb_mech* mech) { delete mech; }
+
+int tchem_gb_mech_host_view(const tchem_gb_mech* mech, tchem_gb_kmcd_view* view) {
+  if (!mech || !view) {
+    set_last_error("tchem_gb_mech_host_view: null argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  *view = mech->view;
+  return TCHEM_GB_OK;
+}
+
+int tchem_gb_mech_species_name(const tchem_gb_mech* mech, int i, char* buf, int buflen) {
+  if (!mech || !buf || buflen <= 0 || i < 0 || i >= mech->km.nSpec) {
+    set_last_error("tchem_gb_mech_species_name: bad argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  std::strncpy(buf, mech->km.speciesNames[i].c_str(), static_cast<size_t>(buflen) - 1);
+  buf[buflen - 1] = '\0';
+  return TCHEM_GB_OK;
+}
+
+int tchem_gb_scenario_batch_size(const char* yaml_path, int* nbatch) {
+  if (!yaml_path || !nbatch) {
+    set_last_error("tchem_gb_scenario_batch_size: null argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  try {
+    // The batch size is the length of environmental_conditions.pressure.initial_value.
+    tchem_gb::KineticModel dummy;
+    dummy.nSpec = 0;
+    std::vector<double> state;
+    tchem_gb::setScenarioConditions(yaml_path, dummy, state, *nbatch);
+    return TCHEM_GB_OK;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return TCHEM_GB_ERR_PARSE;
+  }
+}
+
+int tchem_gb_scenario_read(const char* yaml_path, const tchem_gb_mech* mech, double* state_host, int nbatch) {
+  if (!yaml_path || !mech || !state_host) {
+    set_last_error("tchem_gb_scenario_read: null argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  try {
+    std::vector<double> state;
+    int nb = 0;
+    tchem_gb::setScenarioConditions(yaml_path, mech->km, state, nb);
+    if (nb != nbatch) {
+      set_last_error("tchem_gb_scenario_read: scenario holds " + std::to_string(nb) + " samples, caller passed " +
+                     std::to_string(nbatch));
+      return TCHEM_GB_ERR_ARG;
+    }
+    std::memcpy(state_host, state.data(), state.size() * sizeof(double));
+    return TCHEM_GB_OK;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return TCHEM_GB_ERR_PARSE;
+  }
+}
+
+}  // extern "C"

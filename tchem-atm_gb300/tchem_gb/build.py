@@ -1,0 +1,72 @@
+"""Builds libtchem_gb.so (the engine: sm_103a CUDA kernels + C ABI) in-tree.
+
+Translation units are compiled in parallel with nvcc and linked into
+``tchem-atm_gb300/tchem_gb/libtchem_gb.so``. Nothing here depends on torch.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import shutil
+import subprocess
+import sys
+from pathlib import Path
+
+PKG_DIR = Path(__file__).resolve().parent
+SRC_DIR = PKG_DIR.parent / "csrc"
+BUILD_DIR = PKG_DIR.parent / "_build"
+LIB_PATH = PKG_DIR / "libtchem_gb.so"
+
+ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
+COMMON_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
+
+
+def _nvcc() -> str:
+    cand = shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc"
+    if not Path(cand).exists():
+        raise RuntimeError("nvcc not found: the engine needs the CUDA toolkit to build")
+    return cand
+
+
+def sources() -> list[Path]:
+    return sorted(list(SRC_DIR.glob("*.cu")) + list(SRC_DIR.glob("*.cpp")))
+
+
+def _compile(nvcc: str, src: Path, extra: list[str]) -> Path:
+    obj = BUILD_DIR / (src.name + ".o")
+    cmd = [nvcc, *ARCH_FLAGS, *COMMON_FLAGS, *extra, "-I", str(SRC_DIR), "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if r.stderr.strip():
+        sys.stderr.write(r.stderr)
+    return obj
+
+
+def build(verbose: bool = False, extra_flags: list[str] | None = None, force: bool = False) -> Path:
+    """Compiles every translation unit and links the shared library; returns its path."""
+    nvcc = _nvcc()
+    BUILD_DIR.mkdir(exist_ok=True)
+    srcs = sources()
+    extra = list(extra_flags or [])
+    if not force and LIB_PATH.exists():
+        newest = max(p.stat().st_mtime for p in srcs + list(SRC_DIR.glob("*.h*")) + list(SRC_DIR.glob("*.cuh")))
+        hdr = PKG_DIR.parent.parent / "include" / "tchem_gb.h"
+        if hdr.exists():
+            newest = max(newest, hdr.stat().st_mtime)
+        if LIB_PATH.stat().st_mtime > newest and not extra:
+            return LIB_PATH
+    workers = min(len(srcs), os.cpu_count() or 4)
+    with cf.ThreadPoolExecutor(max_workers=workers) as ex:
+        objs = list(ex.map(lambda s: _compile(nvcc, s, extra), srcs))
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(LIB_PATH), *map(str, objs), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        print(f"built {LIB_PATH}")
+    return LIB_PATH
+
+
+if __name__ == "__main__":
+    build(verbose=True, force="--force" in sys.argv)
