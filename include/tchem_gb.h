@@ -15,7 +15,7 @@
  *                               src/core/TChem_AtmosphericChemistry.cpp:430-508
  *   tchem_gb_workspace_bytes    TChem::AtmosphericChemistry::getWorkSpaceSize
  *                               src/core/TChem_AtmosphericChemistry.hpp:47-81
- *   tchem_gb_time_advance       TChem::AtmosphericChemistry::runDeviceBatch (both overloads)
+  *   tchem_gb_time_advance       TChem::AtmosphericChemistry::runDeviceBatch (both overloads)
  *                               src/core/TChem_AtmosphericChemistry.hpp:83-155,
  *                               src/core/TChem_AtmosphericChemistry.cpp:211-271, 343-385
  *   tchem_gb_kforward           TChem::Impl::KForwardAerosol::team_invoke
@@ -57,18 +57,19 @@ enum tchem_gb_sample_status {
   TCHEM_GB_SAMPLE_SKIPPED = 2,     /* t_out >= t_end on entry: nothing done */
   TCHEM_GB_SAMPLE_NEGATIVE_DT = 3, /* dt_in < 0: returned without touching the outputs */
   TCHEM_GB_SAMPLE_NONFINITE = 4,   /* non-finite value in the state or a step */
-  TCHEM_GB_SAMPLE_DT_UNDERFLOW = 5 /* step size reached 0 before t_end */
+  TCHEM_GB_SAMPLE_DT_UNDERFLOW = 5, /* step size reached 0 before t_end */
+  TCHEM_GB_SAMPLE_BAD_MECH = 6      /* mech_of_sample names no mechanism of the call */
 };
 
 /* Mirrors TChem::TimeAdvance (src/core/TChem_Util.hpp:469-477), same field order and types. */
-typedef struct tchem_gb_time_advance {
+typedef struct tchem_gb_tadv {
   double tbeg, tend;
   double dt, dtmin, dtmax;
   int32_t max_num_newton_iterations;
   int32_t num_time_iterations_per_interval;
   int32_t num_outer_time_iterations_per_interval;
   int32_t jacobian_interval;
-} tchem_gb_time_advance;
+} tchem_gb_tadv;
 
 /* Host view of a parsed mechanism in the reference's table layout
  * (TChem::KineticModelNCAR_ConstData, src/core/TChem_KineticModelNCAR_ConstData.hpp:30-113).
@@ -126,6 +127,69 @@ int tchem_gb_mech_species_name(const tchem_gb_mech* mech, int i, char* buf, int 
 /* Scenario file -> state[nbatch][nSpec+3] on the host ([rho, p, T, x...]). */
 int tchem_gb_scenario_batch_size(const char* yaml_path, int* nbatch);
 int tchem_gb_scenario_read(const char* yaml_path, const tchem_gb_mech* mech, double* state_host, int nbatch);
+
+/* Numerical form of the time advance. */
+enum tchem_gb_form {
+  TCHEM_GB_FORM_PLAIN_FP64 = 0, /* FP64 Newton LU: the parity form */
+  TCHEM_GB_FORM_MIXED = 1       /* FP32 Newton LU and solves, FP64 residual/state/error control */
+};
+
+typedef struct tchem_gb_advance_opts {
+  int32_t form;               /* tchem_gb_form */
+  int32_t threads_per_sample; /* 0: the tuned default for the mechanism */
+  int32_t reserved[6];        /* zero */
+} tchem_gb_advance_opts;
+
+/* Device workspace (bytes) a tchem_gb_time_advance call with these arguments needs. */
+size_t tchem_gb_workspace_bytes(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch,
+                                const tchem_gb_advance_opts* opts);
+
+/* Batched TR-BDF2 time advance of box-model samples on the current CUDA device.
+ * All array arguments are device pointers:
+ *   mechs[n_mechs]     host array of mechanism handles; mech_of_sample[nbatch] selects one per
+ *                      sample (NULL: every sample uses mechs[0]) -- the kmcds overload of the
+ *                      reference; samples of structurally identical mechanisms share a launch.
+ *   tol_newton[2]      Newton {atol, rtol}; tol_time[m_max][2] per-species {atol, rtol}.
+ *   fac                ignored (the Jacobian is analytic); may be NULL.
+ *   tadv[nbatch]       per-sample time-advance controls.
+ *   state[nbatch][nSpec+3] in; state_out may alias state. t_out is read (samples with
+ *                      t_out >= tend are skipped, as the reference does) and written.
+ *   status[nbatch]     tchem_gb_sample_status; stats[nbatch] optional work counters.
+ *   workspace          device scratch of tchem_gb_workspace_bytes() bytes, or NULL to use a
+ *                      library-owned cached allocation (not usable inside stream capture).
+ * Stream-ordered and asynchronous. */
+int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                          const double* tol_newton, const double* tol_time, const double* fac,
+                          const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
+                          double* state_out, int32_t* status, tchem_gb_sample_stats* stats, void* workspace,
+                          size_t workspace_bytes, const tchem_gb_advance_opts* opts, void* stream);
+
+/* Same computation on HOST arrays: copies in, advances, copies out and synchronizes the stream
+ * (the runHostBatch-style entry point for callers without device memory of their own). */
+int tchem_gb_time_advance_hostbuf(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample,
+                                  int nbatch, const double* tol_newton, const double* tol_time,
+                                  const tchem_gb_tadv* tadv, const double* state, double* t_out,
+                                  double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats,
+                                  const tchem_gb_advance_opts* opts, void* stream);
+
+/* Synchronizes `stream`, then reads and clears the device error word of `workspace` (NULL: the
+ * library-owned workspace). *device_error is 0 when no kernel reported a timed-out wait. */
+int tchem_gb_device_error(void* workspace, void* stream, int32_t* device_error);
+
+/* Unit entry points on device arrays (state[nbatch][nSpec+3]):
+ *   kfor[nbatch][nReac] rate constants, omega[nbatch][m] net production rates (active species),
+ *   jac[nbatch][m][m] d omega / d x (row-major). All mechanisms must share one structure. */
+int tchem_gb_kforward(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                      const double* state, double* kfor, void* stream);
+int tchem_gb_reaction_rates(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample,
+                            int nbatch, const double* state, double* omega, void* stream);
+int tchem_gb_jacobian(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                      const double* state, double* jac, void* stream);
+
+/* Measurement helper (no counterpart in the reference): FMA throughput of the current device in
+ * FLOP/s for FP64 (fp64 = 1) or FP32, from independent FMA chains on every SM. These are the
+ * roofline denominators of the FP64-bound plain form and the FP32-bound mixed form. */
+int tchem_gb_measure_fma_peak(int fp64, int blocks_per_sm, int iters, double* flops_per_s);
 
 #ifdef __cplusplus
 }

@@ -71,8 +71,11 @@ class Oracle:
 
     def time_advance(self, tadv: np.ndarray, state: np.ndarray, tol_newton, tol_time: np.ndarray,
                      t_out: np.ndarray | None = None, mech_of_sample: np.ndarray | None = None,
-                     lu_fp32: bool = False, nthreads: int = 0):
-        """Returns (state_out, t_out, dt_out, status, stats)."""
+                     lu_fp32: int = 0, nthreads: int = 0):
+        """Returns (state_out, t_out, dt_out, status, stats).
+
+        lu_fp32: 0 FP64 LU; k >= 1 FP32 LU with k - 1 refinement sweeps after Newton convergence.
+        """
         B = state.shape[0]
         state = np.ascontiguousarray(state, dtype=np.float64)
         state_out = state.copy()

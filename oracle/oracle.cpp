@@ -170,7 +170,7 @@ struct DenseLU {
 };
 
 struct Settings {
-  int max_newton, jac_interval, max_iters;
+  int max_newton, jac_interval, max_iters, refine;
   double atol_newton, rtol_newton;
   const double* tol_time;  // [m][2]
 };
@@ -227,7 +227,17 @@ struct Sample {
       }
       const double ndx = std::sqrt(sdx), ny = std::sqrt(sy);
       if (!std::isfinite(ndx) || !std::isfinite(ny)) return false;
-      if (ndx <= s.atol_newton + s.rtol_newton * ny) return true;
+      if (ndx <= s.atol_newton + s.rtol_newton * ny) {
+        // Refinement sweeps of the mixed algorithm: FP64 residual, solve with the last factors.
+        for (int k = 0; k < s.refine; ++k) {
+          f(y, fy.data());
+          for (int i = 0; i < m; ++i) g[i] = -((y[i] - c * fy[i]) - rhs[i]);
+          lu.solve(g.data(), dx.data());
+          ++st.n_solve;
+          for (int i = 0; i < m; ++i) y[i] += dx[i];
+        }
+        return true;
+      }
     }
     return false;
   }
@@ -307,13 +317,13 @@ struct Sample {
 
 template <typename LU_T>
 void run_batch(const tchem_gb_kmcd_view* const* kms, const int32_t* mech_of_sample, int nbatch, const double* tol_newton,
-               const double* tol_time, const tchem_gb_time_advance* tadv, const double* state, double* t_out,
-               double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats) {
+               const double* tol_time, const tchem_gb_tadv* tadv, const double* state, double* t_out,
+               double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats, int dim, int refine) {
 #pragma omp parallel for schedule(dynamic, 1)
   for (int b = 0; b < nbatch; ++b) {
     const tchem_gb_kmcd_view& km = *kms[mech_of_sample ? mech_of_sample[b] : 0];
-    const int n = km.nSpec, m = km.nSpec - km.nConstSpec, dim = n + 3;
-    const tchem_gb_time_advance& ta = tadv[b];
+    const int n = km.nSpec, m = km.nSpec - km.nConstSpec;
+    const tchem_gb_tadv& ta = tadv[b];
     tchem_gb_sample_stats st0{};
     if (stats) stats[b] = st0;
     if (t_out[b] >= ta.tend) {
@@ -327,7 +337,7 @@ void run_batch(const tchem_gb_kmcd_view* const* kms, const int32_t* mech_of_samp
     std::vector<double> xconst(row + 3 + m, row + 3 + n);
     Sample<LU_T> smp(km, T, p, xconst.data());
     Settings s{ta.max_num_newton_iterations, std::max(1, ta.jacobian_interval), ta.num_time_iterations_per_interval,
-               tol_newton[0], tol_newton[1], tol_time};
+               refine, tol_newton[0], tol_newton[1], tol_time};
     double to = 0.0, dto = 0.0;
     const int st = smp.integrate(y.data(), ta.tbeg, ta.tend, ta.dt, ta.dtmin, ta.dtmax, s, to, dto);
     if (status) status[b] = st;
@@ -370,7 +380,7 @@ int oracle_jacobian(const tchem_gb_kmcd_view* km, double T, double p, const doub
 }
 
 int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const int32_t* mech_of_sample, int nbatch,
-                        const double* tol_newton, const double* tol_time, const tchem_gb_time_advance* tadv,
+                        const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
                         const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
                         tchem_gb_sample_stats* stats, int lu_fp32, int nthreads) {
   if (!kms || n_mechs <= 0 || nbatch < 0 || !tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out ||
@@ -379,14 +389,19 @@ int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const
   if (mech_of_sample)
     for (int b = 0; b < nbatch; ++b)
       if (mech_of_sample[b] < 0 || mech_of_sample[b] >= n_mechs) return TCHEM_GB_ERR_ARG;
+  // Every row has the width of the widest mechanism (one state array for all samples).
+  int dim = 0;
+  for (int i = 0; i < n_mechs; ++i) dim = std::max(dim, kms[i]->nSpec + 3);
 #ifdef _OPENMP
   const int prev = omp_get_max_threads();
   if (nthreads > 0) omp_set_num_threads(nthreads);
 #endif
   if (lu_fp32)
-    run_batch<float>(kms, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status, stats);
+    run_batch<float>(kms, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status,
+                     stats, dim, lu_fp32 - 1);
   else
-    run_batch<double>(kms, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status, stats);
+    run_batch<double>(kms, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status,
+                      stats, dim, 0);
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(prev);
 #endif

@@ -42,12 +42,13 @@ int oracle_jacobian(const tchem_gb_kmcd_view* km, double T, double p, const doub
 
 /* Batched time advance with the reference's runDeviceBatch semantics on host arrays.
  * kms[n_mechs] with mech_of_sample[nbatch] (NULL: every sample uses kms[0]).
- * lu_fp32 = 0: FP64 Newton LU (the plain form); 1: FP32 LU and solves with FP64 residuals
- * (the algorithm of the engine's mixed-precision form, for like-for-like checks).
+ * lu_fp32 = 0: FP64 Newton LU (the plain form); k >= 1: FP32 LU and solves with FP64 residuals
+ * and k - 1 refinement sweeps after Newton convergence (the algorithm of the engine's
+ * mixed-precision form, for like-for-like checks).
  * t_out is read (samples with t_out >= tend are skipped) and written.
  * nthreads <= 0 uses all OpenMP threads. stats may be NULL. */
 int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const int32_t* mech_of_sample, int nbatch,
-                        const double* tol_newton, const double* tol_time, const tchem_gb_time_advance* tadv,
+                        const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
                         const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
                         tchem_gb_sample_stats* stats, int lu_fp32, int nthreads);
 

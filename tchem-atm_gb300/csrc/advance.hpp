@@ -1,0 +1,41 @@
+// Launch parameters of the time-advance kernels (shared by host launch code and kernels).
+#pragma once
+
+#include <cstdint>
+
+#include "../../include/tchem_gb.h"
+#include "device_tables.hpp"
+
+namespace tchem_gb {
+
+constexpr int kMaxMechs = 64;       // mechanisms per time-advance call
+constexpr int kMaxGroupSlots = 8;   // structure-compatible mechanisms sharing one launch
+
+struct AdvanceParams {
+  MechDev mech;                                 // tables of the group (shared structure)
+  const double* rate_param[kMaxGroupSlots];     // per slot: [R][8] rate parameters
+  int32_t slot_of_mech[kMaxMechs];              // global mechanism index -> slot (-1: other group)
+  const int32_t* mech_of_sample;                // [B] or null (all samples use mechanism 0)
+  const int32_t* items;                         // samples of this launch, or null (identity over n_items)
+  const int32_t* n_items_dev;                   // device-side item count, or null (use n_items)
+  int32_t n_items;
+  int32_t* queue;                               // work-queue head, 0 at launch
+  const double* tol_newton;                     // [2]
+  const double* tol_time;                       // [m][2]
+  const tchem_gb_tadv* tadv;                    // [B]
+  const double* state;                          // [B][state_dim]
+  double* state_out;                            // [B][state_dim] (may alias state)
+  double* t_out;                                // [B] in/out
+  double* dt_out;                               // [B]
+  int32_t* status;                              // [B]
+  tchem_gb_sample_stats* stats;                 // [B] or null
+  int32_t state_dim;
+  double* gmat;                                 // per-warp matrix slots in global memory (when not in smem)
+  int64_t gmat_stride;                          // elements per slot
+  int32_t lda;
+  int32_t matrix_in_smem;
+  uint32_t warp_smem_bytes;
+  int32_t* error_word;                          // device-side error report (bounded waits)
+};
+
+}  // namespace tchem_gb

@@ -1,0 +1,507 @@
+// C ABI: device entry points (time advance, unit kernels, workspace planning).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "advance.hpp"
+#include "kernels.hpp"
+#include "kernels_mixed.hpp"
+#include "mech_host.hpp"
+
+namespace tchem_gb {
+
+namespace {
+
+constexpr int kMaxGroups = 16;
+constexpr size_t kHeaderBytes = 256;  // queue[16] @0, error word @64, counts[16] @128
+constexpr int kMaxWarpsPerBlock = 8;
+
+size_t up256(size_t b) { return (b + 255) & ~size_t(255); }
+
+struct DeviceInfo {
+  int sm_count = 0;
+  int max_smem_optin = 0;
+};
+
+DeviceInfo device_info(int dev) {
+  static std::mutex mu;
+  static std::vector<DeviceInfo> cache;
+  std::lock_guard<std::mutex> lk(mu);
+  if (static_cast<int>(cache.size()) <= dev) cache.resize(dev + 1);
+  if (cache[dev].sm_count == 0) {
+    cudaDeviceGetAttribute(&cache[dev].sm_count, cudaDevAttrMultiProcessorCount, dev);
+    cudaDeviceGetAttribute(&cache[dev].max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  }
+  return cache[dev];
+}
+
+DeviceTables* tables_for(const tchem_gb_mech* mech, int dev) {
+  auto* m = const_cast<tchem_gb_mech*>(mech);
+  std::lock_guard<std::mutex> lk(m->mu);
+  if (!m->host_tables) m->host_tables.reset(new HostTables(build_host_tables(m->km)));
+  if (static_cast<int>(m->device_tables.size()) <= dev) m->device_tables.resize(dev + 1, nullptr);
+  if (!m->device_tables[dev]) m->device_tables[dev] = upload_tables(*m->host_tables, dev);
+  return m->device_tables[dev];
+}
+
+struct GroupPlan {
+  std::vector<int> mechs;  // global mechanism indices in slot order
+  MechDev dev{};
+  const void* kernel = nullptr;
+  int form = 0;
+  int warps_per_block = 0;
+  int grid = 0;
+  size_t smem = 0;
+  int lda = 0;
+  bool matrix_in_smem = true;
+  uint32_t warp_smem = 0;
+  size_t gmat_offset = 0;
+  size_t gmat_elems_per_warp = 0;
+  int threads_per_sample = 32;
+};
+
+struct Plan {
+  std::vector<GroupPlan> groups;
+  bool need_items = false;
+  size_t items_offset = 0;
+  size_t bytes = 0;
+  int m_max = 0;
+};
+
+// Groups structurally identical mechanisms and sizes each group's launch.
+Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool have_mos, const tchem_gb_advance_opts& o,
+               int dev) {
+  if (n_mechs <= 0 || n_mechs > kMaxMechs) throw std::invalid_argument("n_mechs must be in [1, 64]");
+  Plan plan;
+  std::vector<const HostTables*> hts(n_mechs);
+  std::vector<DeviceTables*> dts(n_mechs);
+  for (int i = 0; i < n_mechs; ++i) {
+    if (!mechs[i]) throw std::invalid_argument("null mechanism handle");
+    dts[i] = tables_for(mechs[i], dev);
+    hts[i] = mechs[i]->host_tables.get();
+    if (!hts[i]->supported) throw std::domain_error(hts[i]->unsupported_reason);
+  }
+  for (int i = 0; i < n_mechs; ++i) {
+    bool placed = false;
+    for (auto& g : plan.groups) {
+      if (static_cast<int>(g.mechs.size()) < kMaxGroupSlots && hts[g.mechs[0]]->signature == hts[i]->signature) {
+        g.mechs.push_back(i);
+        placed = true;
+        break;
+      }
+    }
+    if (!placed) {
+      if (static_cast<int>(plan.groups.size()) >= kMaxGroups) throw std::invalid_argument("too many mechanism groups");
+      GroupPlan g;
+      g.mechs.push_back(i);
+      g.dev = dts[i]->dev;
+      plan.groups.push_back(g);
+    }
+  }
+  plan.need_items = have_mos && plan.groups.size() > 1;
+  size_t off = kHeaderBytes;
+  if (plan.need_items) {
+    plan.items_offset = off;
+    off += up256(sizeof(int32_t) * static_cast<size_t>(plan.groups.size()) * std::max(nbatch, 1));
+  }
+  const DeviceInfo info = device_info(dev);
+  for (auto& g : plan.groups) {
+    const MechLayout& L = g.dev.L;
+    plan.m_max = std::max(plan.m_max, L.m);
+    g.form = o.form;
+    if (o.form == TCHEM_GB_FORM_MIXED) {
+      MixedConfig mc = mixed_config(L, o.threads_per_sample, info.sm_count, info.max_smem_optin, nbatch);
+      g.kernel = mc.kernel;
+      g.warps_per_block = mc.warps_per_block;
+      g.grid = mc.grid;
+      g.smem = mc.smem;
+      g.threads_per_sample = mc.threads_per_sample;
+      g.matrix_in_smem = true;
+      g.lda = L.m;
+      continue;
+    }
+    g.lda = L.m | 1;
+    size_t ws = fp64_warp_smem_bytes(L, g.lda, true);
+    const size_t avail = static_cast<size_t>(info.max_smem_optin) - 16 - L.blob_bytes;
+    int W = static_cast<int>(std::min<size_t>(kMaxWarpsPerBlock, avail / ws));
+    if (W < 1) {
+      g.matrix_in_smem = false;
+      ws = fp64_warp_smem_bytes(L, g.lda, false);
+      W = static_cast<int>(std::min<size_t>(kMaxWarpsPerBlock, avail / ws));
+      if (W < 1) throw std::invalid_argument("mechanism too large for the shared-memory working set");
+    }
+    g.warp_smem = static_cast<uint32_t>(ws);
+    g.warps_per_block = W;
+    g.smem = 16 + L.blob_bytes + static_cast<size_t>(W) * ws;
+    g.kernel = trbdf2_fp64_kernel_ptr(L.m);
+    cudaFuncSetAttribute(g.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(g.smem));
+    int bps = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, g.kernel, W * 32, g.smem) != cudaSuccess || bps < 1) bps = 1;
+    const int need = (std::max(nbatch, 1) + W - 1) / W;
+    g.grid = std::max(1, std::min(info.sm_count * bps, need));
+    if (!g.matrix_in_smem) {
+      g.gmat_elems_per_warp = static_cast<size_t>(L.m) * g.lda;
+      g.gmat_offset = off;
+      off += up256(sizeof(double) * g.gmat_elems_per_warp * static_cast<size_t>(g.grid) * W);
+    }
+  }
+  plan.bytes = off;
+  return plan;
+}
+
+// Library-owned workspace per device (used when the caller passes none).
+struct OwnedWorkspace {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+std::mutex g_ws_mu;
+std::vector<OwnedWorkspace> g_ws;
+
+void* owned_workspace(int dev, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  if (static_cast<int>(g_ws.size()) <= dev) g_ws.resize(dev + 1);
+  OwnedWorkspace& w = g_ws[dev];
+  if (w.bytes < bytes) {
+    if (w.ptr) {
+      cudaDeviceSynchronize();
+      cudaFree(w.ptr);
+      w.ptr = nullptr;
+      w.bytes = 0;
+    }
+    const size_t want = std::max(bytes, size_t(1) << 20);
+    if (cudaMalloc(&w.ptr, want) != cudaSuccess) {
+      cudaGetLastError();
+      throw std::bad_alloc();
+    }
+    w.bytes = want;
+  }
+  return w.ptr;
+}
+
+void* owned_workspace_peek(int dev) {
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  return static_cast<int>(g_ws.size()) > dev ? g_ws[dev].ptr : nullptr;
+}
+
+int fail(int code, const std::string& msg) {
+  set_last_error(msg);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(TCHEM_GB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+tchem_gb_advance_opts opts_or_default(const tchem_gb_advance_opts* opts) {
+  tchem_gb_advance_opts o{};
+  if (opts) o = *opts;
+  return o;
+}
+
+void fill_slots(const GroupPlan& g, const tchem_gb_mech* const* mechs, int dev, int n_mechs,
+                const double* (&rate_param)[kMaxGroupSlots], int32_t (&slot_of_mech)[kMaxMechs]) {
+  for (int i = 0; i < kMaxGroupSlots; ++i) rate_param[i] = nullptr;
+  for (int i = 0; i < kMaxMechs; ++i) slot_of_mech[i] = -1;
+  for (size_t s = 0; s < g.mechs.size(); ++s) {
+    const int gm = g.mechs[s];
+    rate_param[s] = mechs[gm]->device_tables[dev]->dev.rate_param;
+    if (gm < n_mechs) slot_of_mech[gm] = static_cast<int32_t>(s);
+  }
+}
+
+}  // namespace
+
+}  // namespace tchem_gb
+
+using namespace tchem_gb;
+
+extern "C" {
+
+size_t tchem_gb_workspace_bytes(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch,
+                                const tchem_gb_advance_opts* opts) {
+  try {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const Plan p = make_plan(mechs, n_mechs, nbatch, n_mechs > 1, opts_or_default(opts), dev);
+    return p.bytes;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return 0;
+  }
+}
+
+int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                          const double* tol_newton, const double* tol_time, const double* /*fac*/,
+                          const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
+                          double* state_out, int32_t* status, tchem_gb_sample_stats* stats, void* workspace,
+                          size_t workspace_bytes, const tchem_gb_advance_opts* opts, void* stream_v) {
+  if (!mechs || nbatch < 0) return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance: bad mechanisms or batch size");
+  if (nbatch == 0) return TCHEM_GB_OK;  // empty arrays may come with null pointers
+  if (!tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out || !state_out || !status)
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance: null argument");
+  const tchem_gb_advance_opts o = opts_or_default(opts);
+  if (o.form != TCHEM_GB_FORM_PLAIN_FP64 && o.form != TCHEM_GB_FORM_MIXED)
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance: unknown form");
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  Plan plan;
+  try {
+    plan = make_plan(mechs, n_mechs, nbatch, mech_of_sample != nullptr, o, dev);
+    const int n0 = mechs[0]->km.nSpec;
+    for (int i = 1; i < n_mechs; ++i)
+      if (mechs[i]->km.nSpec + 3 > n0 + 3 && mech_of_sample == nullptr)
+        throw std::invalid_argument("mechanisms of different sizes need mech_of_sample");
+  } catch (const std::domain_error& e) {
+    return fail(TCHEM_GB_ERR_UNSUPPORTED, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(TCHEM_GB_ERR_NOMEM, "tchem_gb_time_advance: allocation failed");
+  } catch (const std::exception& e) {
+    return fail(TCHEM_GB_ERR_ARG, e.what());
+  }
+  // All samples share one state row width: the widest mechanism's nSpec + 3.
+  int state_dim = 0;
+  for (int i = 0; i < n_mechs; ++i) state_dim = std::max(state_dim, mechs[i]->km.nSpec + 3);
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  if (!ws) {
+    try {
+      ws = static_cast<unsigned char*>(owned_workspace(dev, plan.bytes));
+    } catch (...) {
+      return fail(TCHEM_GB_ERR_NOMEM, "tchem_gb_time_advance: workspace allocation failed");
+    }
+  } else if (workspace_bytes < plan.bytes) {
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance: workspace smaller than tchem_gb_workspace_bytes()");
+  }
+  int32_t* queue = reinterpret_cast<int32_t*>(ws);
+  int32_t* error_word = reinterpret_cast<int32_t*>(ws + 64);
+  int32_t* counts = reinterpret_cast<int32_t*>(ws + 128);
+  cudaError_t e = cudaMemsetAsync(ws, 0, 64, stream);  // queues (the error word persists until read)
+  if (e == cudaSuccess) e = cudaMemsetAsync(ws + 128, 0, 64, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(workspace)");
+  int32_t* items = plan.need_items ? reinterpret_cast<int32_t*>(ws + plan.items_offset) : nullptr;
+  if (plan.need_items) {
+    GroupMap G{};
+    for (int i = 0; i < kMaxMechs; ++i) G.group_of_mech[i] = 0;
+    for (size_t g = 0; g < plan.groups.size(); ++g)
+      for (int gm : plan.groups[g].mechs) G.group_of_mech[gm] = static_cast<int32_t>(g);
+    e = launch_bucket(mech_of_sample, nbatch, G, n_mechs, counts, items, status, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "bucket kernel");
+  }
+  for (size_t g = 0; g < plan.groups.size(); ++g) {
+    const GroupPlan& gp = plan.groups[g];
+    AdvanceParams P{};
+    P.mech = gp.dev;
+    fill_slots(gp, mechs, dev, n_mechs, P.rate_param, P.slot_of_mech);
+    if (!mech_of_sample) {
+      for (int i = 0; i < kMaxMechs; ++i) P.slot_of_mech[i] = -1;
+      P.slot_of_mech[0] = 0;
+    }
+    P.mech_of_sample = mech_of_sample;
+    P.items = plan.need_items ? items + g * static_cast<size_t>(nbatch) : nullptr;
+    P.n_items_dev = plan.need_items ? counts + g : nullptr;
+    P.n_items = nbatch;
+    P.queue = queue + g;
+    P.tol_newton = tol_newton;
+    P.tol_time = tol_time;
+    P.tadv = tadv;
+    P.state = state;
+    P.state_out = state_out;
+    P.t_out = t_out;
+    P.dt_out = dt_out;
+    P.status = status;
+    P.stats = stats;
+    P.state_dim = state_dim;
+    P.gmat = gp.matrix_in_smem ? nullptr : reinterpret_cast<double*>(ws + gp.gmat_offset);
+    P.gmat_stride = static_cast<int64_t>(gp.gmat_elems_per_warp);
+    P.lda = gp.lda;
+    P.matrix_in_smem = gp.matrix_in_smem ? 1 : 0;
+    P.warp_smem_bytes = gp.warp_smem;
+    P.error_word = error_word;
+    if (gp.form == TCHEM_GB_FORM_MIXED)
+      e = launch_trbdf2_mixed(P, gp.dev.L, gp.grid, gp.warps_per_block, gp.smem, gp.threads_per_sample, stream);
+    else
+      e = launch_trbdf2_fp64(P, gp.grid, gp.warps_per_block, gp.smem, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "time-advance kernel launch");
+  }
+  return TCHEM_GB_OK;
+}
+
+int tchem_gb_device_error(void* workspace, void* stream_v, int32_t* device_error) {
+  if (!device_error) return fail(TCHEM_GB_ERR_ARG, "tchem_gb_device_error: null argument");
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+  cudaError_t e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  unsigned char* ws = static_cast<unsigned char*>(workspace ? workspace : owned_workspace_peek(dev));
+  *device_error = 0;
+  if (!ws) return TCHEM_GB_OK;
+  e = cudaMemcpy(device_error, ws + 64, sizeof(int32_t), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemset(ws + 64, 0, sizeof(int32_t));
+  if (e != cudaSuccess) return cuda_fail(e, "tchem_gb_device_error");
+  return TCHEM_GB_OK;
+}
+
+namespace {
+
+struct HostBufCache {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+std::mutex g_hb_mu;
+std::vector<HostBufCache> g_hb;
+
+int run_unit(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+             const double* state, double* out, void* stream_v, UnitKind kind) {
+  if (!mechs || n_mechs <= 0 || n_mechs > kMaxGroupSlots || nbatch < 0)
+    return fail(TCHEM_GB_ERR_ARG, "unit entry point: bad argument");
+  if (nbatch == 0) return TCHEM_GB_OK;
+  if (!state || !out) return fail(TCHEM_GB_ERR_ARG, "unit entry point: null array");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  UnitParams P{};
+  try {
+    const DeviceTables* t0 = tables_for(mechs[0], dev);
+    const HostTables* h0 = mechs[0]->host_tables.get();
+    if (!h0->supported && kind != UNIT_KFORWARD) throw std::domain_error(h0->unsupported_reason);
+    P.mech = t0->dev;
+    for (int i = 0; i < kMaxMechs; ++i) P.slot_of_mech[i] = -1;
+    for (int i = 0; i < n_mechs; ++i) {
+      const DeviceTables* ti = tables_for(mechs[i], dev);
+      if (mechs[i]->host_tables->signature != h0->signature)
+        throw std::invalid_argument("unit entry points need mechanisms of one structure");
+      P.rate_param[i] = ti->dev.rate_param;
+      P.slot_of_mech[i] = i;
+    }
+  } catch (const std::domain_error& e) {
+    return fail(TCHEM_GB_ERR_UNSUPPORTED, e.what());
+  } catch (const std::exception& e) {
+    return fail(TCHEM_GB_ERR_ARG, e.what());
+  }
+  unsigned char* ws = nullptr;
+  try {
+    ws = static_cast<unsigned char*>(owned_workspace(dev, kHeaderBytes));
+  } catch (...) {
+    return fail(TCHEM_GB_ERR_NOMEM, "workspace allocation failed");
+  }
+  P.mech_of_sample = mech_of_sample;
+  P.B = nbatch;
+  P.state = state;
+  P.state_dim = mechs[0]->km.nSpec + 3;
+  P.out = out;
+  P.error_word = reinterpret_cast<int32_t*>(ws + 64);
+  P.status = nullptr;
+  cudaError_t e = launch_unit(P, kind, static_cast<cudaStream_t>(stream_v));
+  if (e != cudaSuccess) return cuda_fail(e, "unit kernel launch");
+  return TCHEM_GB_OK;
+}
+
+}  // namespace
+
+int tchem_gb_kforward(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                      const double* state, double* kfor, void* stream) {
+  return run_unit(mechs, n_mechs, mech_of_sample, nbatch, state, kfor, stream, UNIT_KFORWARD);
+}
+
+int tchem_gb_reaction_rates(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample,
+                            int nbatch, const double* state, double* omega, void* stream) {
+  return run_unit(mechs, n_mechs, mech_of_sample, nbatch, state, omega, stream, UNIT_RHS);
+}
+
+int tchem_gb_jacobian(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                      const double* state, double* jac, void* stream) {
+  return run_unit(mechs, n_mechs, mech_of_sample, nbatch, state, jac, stream, UNIT_JACOBIAN);
+}
+
+int tchem_gb_time_advance_hostbuf(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample,
+                                  int nbatch, const double* tol_newton, const double* tol_time,
+                                  const tchem_gb_tadv* tadv, const double* state, double* t_out,
+                                  double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats,
+                                  const tchem_gb_advance_opts* opts, void* stream_v) {
+  if (!mechs || n_mechs <= 0 || nbatch < 0)
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance_hostbuf: bad mechanisms or batch size");
+  if (nbatch == 0) return TCHEM_GB_OK;
+  if (!tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out || !state_out || !status)
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance_hostbuf: null argument");
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int m_max = 0, dim = 0;
+  for (int i = 0; i < n_mechs; ++i) {
+    if (!mechs[i]) return fail(TCHEM_GB_ERR_ARG, "null mechanism handle");
+    m_max = std::max(m_max, mechs[i]->km.nActive());
+    dim = std::max(dim, mechs[i]->km.nSpec + 3);
+  }
+  const size_t B = static_cast<size_t>(nbatch);
+  size_t off = 0;
+  auto sec = [&](size_t bytes) { const size_t o = off; off += up256(bytes); return o; };
+  const size_t o_tn = sec(2 * sizeof(double));
+  const size_t o_tt = sec(2 * sizeof(double) * m_max);
+  const size_t o_tadv = sec(sizeof(tchem_gb_tadv) * B);
+  const size_t o_state = sec(sizeof(double) * B * dim);
+  const size_t o_sout = sec(sizeof(double) * B * dim);
+  const size_t o_t = sec(sizeof(double) * B);
+  const size_t o_dt = sec(sizeof(double) * B);
+  const size_t o_st = sec(sizeof(int32_t) * B);
+  const size_t o_stats = sec(sizeof(tchem_gb_sample_stats) * B);
+  const size_t o_mos = sec(sizeof(int32_t) * B);
+  unsigned char* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_hb_mu);
+    if (static_cast<int>(g_hb.size()) <= dev) g_hb.resize(dev + 1);
+    HostBufCache& c = g_hb[dev];
+    if (c.bytes < off) {
+      if (c.ptr) {
+        cudaDeviceSynchronize();
+        cudaFree(c.ptr);
+      }
+      c.ptr = nullptr;
+      c.bytes = 0;
+      if (cudaMalloc(&c.ptr, off) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(TCHEM_GB_ERR_NOMEM, "tchem_gb_time_advance_hostbuf: device buffer allocation failed");
+      }
+      c.bytes = off;
+    }
+    base = static_cast<unsigned char*>(c.ptr);
+  }
+  auto h2d = [&](size_t o, const void* src, size_t bytes) {
+    return cudaMemcpyAsync(base + o, src, bytes, cudaMemcpyHostToDevice, stream);
+  };
+  cudaError_t e = h2d(o_tn, tol_newton, 2 * sizeof(double));
+  if (e == cudaSuccess) e = h2d(o_tt, tol_time, 2 * sizeof(double) * m_max);
+  if (e == cudaSuccess) e = h2d(o_tadv, tadv, sizeof(tchem_gb_tadv) * B);
+  if (e == cudaSuccess) e = h2d(o_state, state, sizeof(double) * B * dim);
+  if (e == cudaSuccess) e = h2d(o_t, t_out, sizeof(double) * B);
+  if (e == cudaSuccess && mech_of_sample) e = h2d(o_mos, mech_of_sample, sizeof(int32_t) * B);
+  if (e != cudaSuccess) return cuda_fail(e, "tchem_gb_time_advance_hostbuf: host-to-device copy");
+  // state_out starts as a copy of state so rows of skipped samples come back unchanged.
+  e = cudaMemcpyAsync(base + o_sout, base + o_state, sizeof(double) * B * dim, cudaMemcpyDeviceToDevice, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "tchem_gb_time_advance_hostbuf: device copy");
+  const int rc = tchem_gb_time_advance(
+      mechs, n_mechs, mech_of_sample ? reinterpret_cast<const int32_t*>(base + o_mos) : nullptr, nbatch,
+      reinterpret_cast<const double*>(base + o_tn), reinterpret_cast<const double*>(base + o_tt), nullptr,
+      reinterpret_cast<const tchem_gb_tadv*>(base + o_tadv), reinterpret_cast<const double*>(base + o_state),
+      reinterpret_cast<double*>(base + o_t), reinterpret_cast<double*>(base + o_dt),
+      reinterpret_cast<double*>(base + o_sout), reinterpret_cast<int32_t*>(base + o_st),
+      stats ? reinterpret_cast<tchem_gb_sample_stats*>(base + o_stats) : nullptr, nullptr, 0, opts, stream_v);
+  if (rc != TCHEM_GB_OK) return rc;
+  auto d2h = [&](void* dst, size_t o, size_t bytes) {
+    return cudaMemcpyAsync(dst, base + o, bytes, cudaMemcpyDeviceToHost, stream);
+  };
+  e = d2h(state_out, o_sout, sizeof(double) * B * dim);
+  if (e == cudaSuccess) e = d2h(t_out, o_t, sizeof(double) * B);
+  if (e == cudaSuccess) e = d2h(dt_out, o_dt, sizeof(double) * B);
+  if (e == cudaSuccess) e = d2h(status, o_st, sizeof(int32_t) * B);
+  if (e == cudaSuccess && stats) e = d2h(stats, o_stats, sizeof(tchem_gb_sample_stats) * B);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+  if (e != cudaSuccess) return cuda_fail(e, "tchem_gb_time_advance_hostbuf: device-to-host copy");
+  return TCHEM_GB_OK;
+}
+
+}  // extern "C"

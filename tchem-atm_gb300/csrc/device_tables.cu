@@ -1,0 +1,243 @@
+// Builds and uploads the packed per-mechanism tables (layout in device_tables.hpp).
+#include "device_tables.hpp"
+
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+#include <string>
+
+namespace tchem_gb {
+
+namespace {
+
+size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+template <typename T>
+void put(std::vector<unsigned char>& blob, int32_t off, const std::vector<T>& v) {
+  if (!v.empty()) std::memcpy(blob.data() + off, v.data(), v.size() * sizeof(T));
+}
+
+}  // namespace
+
+HostTables build_host_tables(const KineticModel& km) {
+  HostTables ht;
+  const int m = km.nActive(), n = km.nSpec, R = km.nReac, S = km.maxSpecInReac, joff = S / 2;
+  if (m <= 0) throw std::runtime_error("mechanism has no active species");
+  if (m >= 32768 || R >= 32768) throw std::runtime_error("mechanism too large for the device tables");
+
+  // Rate parameters per reaction.
+  ht.rate_type.assign(R, RATE_ZERO);
+  ht.rate_param.assign(static_cast<size_t>(R) * 8, 0.0);
+  ht.conv_exp.assign(km.convExponent.begin(), km.convExponent.end());
+  for (const auto& a : km.arrhenius) {
+    ht.rate_type[a.reaction_index] = RATE_ARRHENIUS;
+    double* p = &ht.rate_param[static_cast<size_t>(a.reaction_index) * 8];
+    p[0] = a.A; p[1] = a.B; p[2] = a.C; p[3] = a.D; p[4] = a.E;
+  }
+  for (size_t i = 0; i < km.reacPfal.size(); ++i) {
+    const int r = km.reacPfal[i];
+    ht.rate_type[r] = RATE_TROE;
+    for (int k = 0; k < 8; ++k) ht.rate_param[static_cast<size_t>(r) * 8 + k] = km.reacPpar[i * 8 + k];
+  }
+  for (const auto& c : km.cmaq_h2o2) {
+    ht.rate_type[c.reaction_index] = RATE_CMAQ_H2O2;
+    double* p = &ht.rate_param[static_cast<size_t>(c.reaction_index) * 8];
+    p[0] = c.A1; p[1] = c.B1; p[2] = c.C1; p[3] = c.A2; p[4] = c.B2; p[5] = c.C2;
+  }
+  for (int r = 0; r < R; ++r) {
+    const int t = km.reacType[r];
+    if (t == KineticModel::JPL || t == KineticModel::R_JPL_ARRHENIUS || t == KineticModel::PHOTO_RATE) {
+      ht.supported = false;
+      ht.unsupported_reason = "reaction " + std::to_string(r) +
+                              " uses a JPL, R_JPL_ARRHENIUS or PHOTO_RATE rate: the box-model time advance "
+                              "evaluates ARRHENIUS, TROE and CMAQ_H2O2 rates only";
+    }
+  }
+
+  // Factor slots (rate of progress) and constant-species factors.
+  std::vector<int32_t> rf_ptr(R + 1, 0);
+  std::vector<int16_t> rf_sp;
+  ht.cf_ptr.assign(R + 1, 0);
+  int max_factors = 0;
+  for (int r = 0; r < R; ++r) {
+    rf_ptr[r] = static_cast<int32_t>(rf_sp.size());
+    ht.cf_ptr[r] = static_cast<int32_t>(ht.cf_idx.size());
+    for (int j = 0; j < km.reacNreac[r]; ++j) {
+      const int s = km.sidx(r, j);
+      const int pw = std::abs(static_cast<int>(km.nuki(r, j)));
+      for (int k = 0; k < pw; ++k) {
+        if (s < m) rf_sp.push_back(static_cast<int16_t>(s));
+        else ht.cf_idx.push_back(s - m);
+      }
+    }
+    max_factors = std::max(max_factors, static_cast<int>(rf_sp.size()) - rf_ptr[r]);
+  }
+  rf_ptr[R] = static_cast<int32_t>(rf_sp.size());
+  ht.cf_ptr[R] = static_cast<int32_t>(ht.cf_idx.size());
+
+  // Per reaction, the (species, nu) entries in the reference's scatter order: reactant slots,
+  // then product slots; constant species and zero coefficients are skipped.
+  std::vector<std::vector<std::pair<int, double>>> rxn_entries(R);
+  for (int r = 0; r < R; ++r) {
+    for (int j = 0; j < km.reacNreac[r]; ++j) {
+      const int s = km.sidx(r, j);
+      const double nu = km.nuki(r, j);
+      if (s < m && nu != 0.0) rxn_entries[r].push_back({s, nu});
+    }
+    for (int j = 0; j < km.reacNprod[r]; ++j) {
+      const int s = km.sidx(r, j + joff);
+      const double nu = km.nuki(r, j + joff);
+      if (s < m && nu != 0.0) rxn_entries[r].push_back({s, nu});
+    }
+  }
+
+  // Net production CSR over active species, reactions in ascending order.
+  std::vector<std::vector<std::pair<int, double>>> per_species(m);
+  for (int r = 0; r < R; ++r)
+    for (const auto& e : rxn_entries[r]) per_species[e.first].push_back({r, e.second});
+  std::vector<int32_t> pr_ptr(m + 1, 0);
+  std::vector<int16_t> pr_r;
+  std::vector<double> pr_nu;
+  for (int k = 0; k < m; ++k) {
+    pr_ptr[k] = static_cast<int32_t>(pr_r.size());
+    for (const auto& e : per_species[k]) {
+      pr_r.push_back(static_cast<int16_t>(e.first));
+      pr_nu.push_back(e.second);
+    }
+  }
+  pr_ptr[m] = static_cast<int32_t>(pr_r.size());
+
+  // Jacobian nonzeros (row-major) with their contributions.
+  std::map<std::pair<int, int>, std::vector<std::pair<int, double>>> jac;
+  for (int r = 0; r < R; ++r)
+    for (int f = rf_ptr[r]; f < rf_ptr[r + 1]; ++f)
+      for (const auto& e : rxn_entries[r]) jac[{e.first, rf_sp[f]}].push_back({f, e.second});
+  std::vector<int32_t> jz_rc, jz_ptr;
+  std::vector<int16_t> jc_f;
+  std::vector<double> jc_nu;
+  std::vector<float> jc_nu32;
+  for (const auto& kv : jac) {
+    jz_rc.push_back((kv.first.first << 16) | kv.first.second);
+    jz_ptr.push_back(static_cast<int32_t>(jc_f.size()));
+    for (const auto& c : kv.second) {
+      jc_f.push_back(static_cast<int16_t>(c.first));
+      jc_nu.push_back(c.second);
+      jc_nu32.push_back(static_cast<float>(c.second));
+    }
+  }
+  jz_ptr.push_back(static_cast<int32_t>(jc_f.size()));
+
+  std::vector<double> emis(m, 0.0);
+  for (const auto& e : km.emission)
+    if (e.species_index < m) emis[e.species_index] = e.emission_rate;  // last entry wins, as the reference's assignment
+
+  MechLayout& L = ht.L;
+  L.m = m; L.n = n; L.nconst = n - m; L.R = R;
+  L.NF = static_cast<int32_t>(rf_sp.size());
+  L.NP = static_cast<int32_t>(pr_r.size());
+  L.NZ = static_cast<int32_t>(jz_rc.size());
+  L.NC = static_cast<int32_t>(jc_f.size());
+  L.max_factors = max_factors;
+  size_t off = 0;
+  auto sec = [&](size_t bytes) { const int32_t o = static_cast<int32_t>(off); off = align16(off + bytes); return o; };
+  L.off_emis = sec(sizeof(double) * m);
+  L.off_rf_ptr = sec(sizeof(int32_t) * (R + 1));
+  L.off_pr_ptr = sec(sizeof(int32_t) * (m + 1));
+  L.off_pr_nu = sec(sizeof(double) * pr_nu.size());
+  L.off_jz_rc = sec(sizeof(int32_t) * jz_rc.size());
+  L.off_jz_ptr = sec(sizeof(int32_t) * jz_ptr.size());
+  L.off_jc_nu = sec(sizeof(double) * jc_nu.size());
+  L.off_jc_nu32 = sec(sizeof(float) * jc_nu32.size());
+  L.off_rf_sp = sec(sizeof(int16_t) * rf_sp.size());
+  L.off_pr_r = sec(sizeof(int16_t) * pr_r.size());
+  L.off_jc_f = sec(sizeof(int16_t) * jc_f.size());
+  L.blob_bytes = static_cast<int32_t>(align16(off));
+  ht.blob.assign(L.blob_bytes, 0);
+  put(ht.blob, L.off_emis, emis);
+  put(ht.blob, L.off_rf_ptr, rf_ptr);
+  put(ht.blob, L.off_rf_sp, rf_sp);
+  put(ht.blob, L.off_pr_ptr, pr_ptr);
+  put(ht.blob, L.off_pr_r, pr_r);
+  put(ht.blob, L.off_pr_nu, pr_nu);
+  put(ht.blob, L.off_jz_rc, jz_rc);
+  put(ht.blob, L.off_jz_ptr, jz_ptr);
+  put(ht.blob, L.off_jc_f, jc_f);
+  put(ht.blob, L.off_jc_nu, jc_nu);
+  put(ht.blob, L.off_jc_nu32, jc_nu32);
+
+  // Structural signature: everything except the rate parameters.
+  auto mix = [&](int64_t v) { ht.signature.push_back(v); };
+  mix(m); mix(n); mix(R);
+  for (unsigned char b : ht.blob) mix(b);
+  for (int32_t v : ht.cf_ptr) mix(v);
+  for (int32_t v : ht.cf_idx) mix(v);
+  for (int32_t v : ht.conv_exp) mix(v);
+  for (int32_t v : ht.rate_type) mix(v);
+  return ht;
+}
+
+DeviceTables* upload_tables(const HostTables& ht, int device) {
+  const MechLayout& L = ht.L;
+  const size_t R = static_cast<size_t>(L.R);
+  size_t off = 0;
+  auto sec = [&](size_t bytes) { const size_t o = off; off = (off + bytes + 255) & ~size_t(255); return o; };
+  const size_t o_blob = sec(L.blob_bytes);
+  const size_t o_type = sec(sizeof(int32_t) * R);
+  const size_t o_param = sec(sizeof(double) * R * 8);
+  const size_t o_conv = sec(sizeof(int32_t) * R);
+  const size_t o_cfp = sec(sizeof(int32_t) * (R + 1));
+  const size_t o_cfi = sec(sizeof(int32_t) * std::max<size_t>(1, ht.cf_idx.size()));
+  std::vector<unsigned char> host(off, 0);
+  std::memcpy(host.data() + o_blob, ht.blob.data(), ht.blob.size());
+  std::memcpy(host.data() + o_type, ht.rate_type.data(), sizeof(int32_t) * R);
+  std::memcpy(host.data() + o_param, ht.rate_param.data(), sizeof(double) * R * 8);
+  std::memcpy(host.data() + o_conv, ht.conv_exp.data(), sizeof(int32_t) * R);
+  std::memcpy(host.data() + o_cfp, ht.cf_ptr.data(), sizeof(int32_t) * (R + 1));
+  if (!ht.cf_idx.empty()) std::memcpy(host.data() + o_cfi, ht.cf_idx.data(), sizeof(int32_t) * ht.cf_idx.size());
+
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (cudaSetDevice(device) != cudaSuccess) throw std::runtime_error("cudaSetDevice failed");
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, off);
+  if (e != cudaSuccess) {
+    cudaSetDevice(prev);
+    throw std::runtime_error(std::string("cudaMalloc for mechanism tables: ") + cudaGetErrorString(e));
+  }
+  e = cudaMemcpy(p, host.data(), off, cudaMemcpyHostToDevice);
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) {
+    cudaFree(p);
+    throw std::runtime_error(std::string("cudaMemcpy for mechanism tables: ") + cudaGetErrorString(e));
+  }
+  auto* t = new DeviceTables();
+  t->device = device;
+  t->allocation = p;
+  unsigned char* b = static_cast<unsigned char*>(p);
+  t->dev.L = L;
+  t->dev.blob = b + o_blob;
+  t->dev.rate_type = reinterpret_cast<const int32_t*>(b + o_type);
+  t->dev.rate_param = reinterpret_cast<const double*>(b + o_param);
+  t->dev.conv_exp = reinterpret_cast<const int32_t*>(b + o_conv);
+  t->dev.cf_ptr = reinterpret_cast<const int32_t*>(b + o_cfp);
+  t->dev.cf_idx = reinterpret_cast<const int32_t*>(b + o_cfi);
+  t->dev.conv_ppm = CONV_PPM;
+  return t;
+}
+
+void destroy_device_tables(DeviceTables* t) {
+  if (!t) return;
+  if (t->allocation) {
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(t->device);
+    cudaFree(t->allocation);
+    cudaSetDevice(prev);
+  }
+  delete t;
+}
+
+}  // namespace tchem_gb

@@ -1,0 +1,76 @@
+// Packed per-mechanism tables for the device kernels.
+//
+// The reference keeps the mechanism as arrays-of-structs read from global memory on every
+// RHS call (KineticModelNCAR_ConstData, src/core/TChem_KineticModelNCAR_ConstData.hpp:30-113)
+// and recomputes every rate constant inside every RHS call
+// (src/core/impl/TChem_Impl_ReactionRatesAerosol.hpp:96). Here the mechanism is compiled once
+// into three small sparse programs that a CTA stages into shared memory with one bulk copy:
+//
+//  * rate of progress: for reaction r, q_r = keff_r * prod_{f in [rf_ptr[r], rf_ptr[r+1])} x[rf_sp[f]]
+//    where every active reactant appears |nu| times and keff_r folds the rate constant and the
+//    (per-sample constant) concentrations of constant species;
+//  * net production (CSR over active species k): omega_k = emis_k + sum_e pr_nu[e] * q[pr_r[e]];
+//  * analytic Jacobian: for each factor slot f, d_f = keff_r * prod_{g != f} x[rf_sp[g]] is
+//    dq_r/dx along that slot; Jacobian nonzero z = (jz_row[z], jz_col[z]) accumulates
+//    J_z = sum_{c in [jz_ptr[z], jz_ptr[z+1])} jc_nu[c] * d[jc_f[c]].
+//
+// Rate-constant parameters stay in global memory: they are read once per sample.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+#include "kinetic_model.hpp"
+
+namespace tchem_gb {
+
+enum DevRateType : int32_t { RATE_ARRHENIUS = 0, RATE_TROE = 1, RATE_CMAQ_H2O2 = 2, RATE_ZERO = 3 };
+
+// Byte offsets of each section inside the staged blob (16-byte aligned sections).
+struct MechLayout {
+  int32_t m, n, nconst, R, NF, NP, NZ, NC;
+  int32_t off_rf_ptr, off_rf_sp;            // int32[R+1], int16[NF]
+  int32_t off_pr_ptr, off_pr_r, off_pr_nu;  // int32[m+1], int16[NP], double[NP]
+  int32_t off_jz_rc, off_jz_ptr;            // int32[NZ] (row<<16 | col), int32[NZ+1]
+  int32_t off_jc_f, off_jc_nu, off_jc_nu32;  // int16[NC], double[NC], float[NC]
+  int32_t off_emis;                         // double[m]
+  int32_t blob_bytes;                       // multiple of 16
+  int32_t max_factors;                      // max factor slots of one reaction
+};
+
+// Device pointers of one mechanism on one device (passed by value to kernels).
+struct MechDev {
+  MechLayout L;
+  const unsigned char* blob;  // staged tables (global copy, 256-byte aligned)
+  const int32_t* rate_type;   // [R]
+  const double* rate_param;   // [R][8]
+  const int32_t* conv_exp;    // [R]
+  const int32_t* cf_ptr;      // [R+1] constant-species factors of reaction r
+  const int32_t* cf_idx;      // constant-species slot (0..nconst-1), one entry per unit of |nu|
+  double conv_ppm;
+};
+
+// Host-side packed tables, built from a parsed kinetic model.
+struct HostTables {
+  MechLayout L{};
+  std::vector<unsigned char> blob;
+  std::vector<int32_t> rate_type, conv_exp, cf_ptr, cf_idx;
+  std::vector<double> rate_param;
+  // Structural signature: mechanisms with equal signatures share one kernel launch.
+  std::vector<int64_t> signature;
+  bool supported = true;     // false when the mechanism has rate types outside the box path
+  std::string unsupported_reason;
+};
+
+HostTables build_host_tables(const KineticModel& km);
+
+struct DeviceTables {
+  int device = -1;
+  MechDev dev{};
+  void* allocation = nullptr;
+};
+
+DeviceTables* upload_tables(const HostTables& ht, int device);
+void destroy_device_tables(DeviceTables* t);
+
+}  // namespace tchem_gb

@@ -1,0 +1,39 @@
+// Host-callable launchers of the device kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "advance.hpp"
+
+namespace tchem_gb {
+
+// Plain FP64 form (kernels_fp64.cu).
+size_t fp64_warp_smem_bytes(const MechLayout& L, int lda, bool matrix_in_smem);
+cudaError_t launch_trbdf2_fp64(const AdvanceParams& P, int grid, int warps_per_block, size_t smem,
+                               cudaStream_t stream);
+const void* trbdf2_fp64_kernel_ptr(int m);
+
+// Unit kernels on the same tables (kernels_fp64.cu): one warp per sample.
+struct UnitParams {
+  MechDev mech;
+  const double* rate_param[kMaxGroupSlots];
+  int32_t slot_of_mech[kMaxMechs];
+  const int32_t* mech_of_sample;
+  int32_t B;
+  const double* state;  // [B][state_dim]
+  int32_t state_dim;
+  double* out;          // kforward [B][R], rhs [B][m], jacobian [B][m][m]
+  int32_t* error_word;
+  int32_t* status;      // [B] or null: TCHEM_GB_SAMPLE_BAD_MECH for samples with no mechanism
+};
+enum UnitKind { UNIT_KFORWARD = 0, UNIT_RHS = 1, UNIT_JACOBIAN = 2 };
+cudaError_t launch_unit(const UnitParams& P, UnitKind kind, cudaStream_t stream);
+
+// Groups samples by mechanism group: items[g * B + k], counts[g] (kernels_fp64.cu).
+struct GroupMap {
+  int32_t group_of_mech[kMaxMechs];
+};
+cudaError_t launch_bucket(const int32_t* mech_of_sample, int B, const GroupMap& G, int n_mechs,
+                          int32_t* counts, int32_t* items, int32_t* status, cudaStream_t stream);
+
+}  // namespace tchem_gb

@@ -1,0 +1,86 @@
+// Mixed-precision form: kernel-shape selection and launch configuration for the register-resident
+// FP32-LU kernel (kernels_mixed_impl.cuh).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <stdexcept>
+
+#include "kernels_mixed.hpp"
+#include "kernels_mixed_impl.cuh"
+
+namespace tchem_gb {
+
+// Launchers defined in kernels_mixed_v*.cu (one translation unit per kernel shape).
+cudaError_t launch_mixed_24_1(const AdvanceParams&, int, int, size_t, cudaStream_t);
+const void* kernel_mixed_24_1();
+cudaError_t launch_mixed_32_1(const AdvanceParams&, int, int, size_t, cudaStream_t);
+const void* kernel_mixed_32_1();
+cudaError_t launch_mixed_52_2(const AdvanceParams&, int, int, size_t, cudaStream_t);
+const void* kernel_mixed_52_2();
+cudaError_t launch_mixed_64_2(const AdvanceParams&, int, int, size_t, cudaStream_t);
+const void* kernel_mixed_64_2();
+
+namespace {
+
+constexpr int kMaxWarps = 8;
+
+struct Variant {
+  int MC, RPT;
+  const void* kernel;
+  cudaError_t (*launch)(const AdvanceParams&, int, int, size_t, cudaStream_t);
+};
+
+// Kernel shapes (columns, rows per lane); a mechanism uses the narrowest with MC >= m and
+// 32 * RPT >= m.
+const Variant* variants(int* n) {
+  static const Variant v[] = {
+      {24, 1, kernel_mixed_24_1(), &launch_mixed_24_1},
+      {32, 1, kernel_mixed_32_1(), &launch_mixed_32_1},
+      {52, 2, kernel_mixed_52_2(), &launch_mixed_52_2},
+      {64, 2, kernel_mixed_64_2(), &launch_mixed_64_2},
+  };
+  *n = static_cast<int>(sizeof(v) / sizeof(v[0]));
+  return v;
+}
+
+const Variant* pick(const MechLayout& L) {
+  int nv = 0;
+  const Variant* v = variants(&nv);
+  for (int i = 0; i < nv; ++i)
+    if (v[i].MC >= L.m && 32 * v[i].RPT >= L.m) return &v[i];
+  return nullptr;
+}
+
+}  // namespace
+
+MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch) {
+  if (threads_per_sample != 0 && threads_per_sample != 32)
+    throw std::domain_error("mixed form: threads_per_sample must be 0 or 32");
+  const Variant* best = pick(L);
+  if (!best) throw std::domain_error("mixed form: mechanisms with more than 64 active species are not supported");
+  const size_t gbytes = mixed::group_smem_bytes(L, best->MC);
+  const size_t avail = static_cast<size_t>(max_smem_optin) - 16 - L.blob_bytes;
+  const int warps = static_cast<int>(std::min<size_t>(kMaxWarps, avail / gbytes));
+  if (warps < 1) throw std::domain_error("mixed form: shared-memory working set too large");
+  MixedConfig mc;
+  mc.kernel = best->kernel;
+  mc.threads_per_sample = 32;
+  mc.warps_per_block = warps;
+  mc.smem = 16 + L.blob_bytes + warps * gbytes;
+  cudaFuncSetAttribute(mc.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(mc.smem));
+  int bps = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, mc.kernel, warps * 32, mc.smem) != cudaSuccess || bps < 1)
+    bps = 1;
+  const int need = (std::max(nbatch, 1) + warps - 1) / warps;
+  mc.grid = std::max(1, std::min(sm_count * bps, need));
+  return mc;
+}
+
+cudaError_t launch_trbdf2_mixed(const AdvanceParams& P, const MechLayout& L, int grid, int warps_per_block,
+                                size_t smem, int /*threads_per_sample*/, cudaStream_t stream) {
+  const Variant* best = pick(L);
+  if (!best) return cudaErrorInvalidValue;
+  return best->launch(P, grid, warps_per_block * 32, smem, stream);
+}
+
+}  // namespace tchem_gb

@@ -1,0 +1,23 @@
+// Mixed-precision form: FP32 Newton LU and solves held in registers, FP64 residual, state and
+// error control.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "advance.hpp"
+
+namespace tchem_gb {
+
+struct MixedConfig {
+  const void* kernel = nullptr;
+  int warps_per_block = 0;
+  int grid = 0;
+  size_t smem = 0;
+  int threads_per_sample = 32;
+};
+
+MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch);
+cudaError_t launch_trbdf2_mixed(const AdvanceParams& P, const MechLayout& L, int grid, int warps_per_block,
+                                size_t smem, int threads_per_sample, cudaStream_t stream);
+
+}  // namespace tchem_gb

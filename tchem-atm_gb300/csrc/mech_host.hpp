@@ -6,11 +6,12 @@
 #include <vector>
 
 #include "../../include/tchem_gb.h"
+#include "device_tables.hpp"
 #include "kinetic_model.hpp"
+#include <memory>
+#include <mutex>
 
 namespace tchem_gb {
-
-struct DeviceTables;  // device-resident packed tables (engine.cuh)
 
 // Thread-local last-error message for tchem_gb_last_error().
 void set_last_error(const std::string& msg);
@@ -23,8 +24,10 @@ struct tchem_gb_mech {
   std::vector<int32_t> arrhenius_reaction, cmaq_reaction, emission_species, reacPfal;
   std::vector<double> arrhenius_param, cmaq_param, emission_rate;
   tchem_gb_kmcd_view view{};
-  // Device tables per CUDA device ordinal (built on first use on that device).
+  // Packed tables (built on first device use) and their device copies per CUDA device ordinal.
+  std::unique_ptr<tchem_gb::HostTables> host_tables;
   std::vector<tchem_gb::DeviceTables*> device_tables;
+  std::mutex mu;
 
   void build_view();
   ~tchem_gb_mech();

@@ -42,6 +42,10 @@ class KmcdView(C.Structure):
     ]
 
 
+class AdvanceOpts(C.Structure):
+    _fields_ = [("form", C.c_int32), ("threads_per_sample", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
 class TChemGBError(RuntimeError):
     """Error returned by the engine's C ABI (message from tchem_gb_last_error)."""
 
@@ -74,21 +78,25 @@ def lib() -> C.CDLL:
         "tchem_gb_scenario_batch_size": (C.c_int, [C.c_char_p, C.POINTER(C.c_int)]),
         "tchem_gb_scenario_read": (C.c_int, [C.c_char_p, vp, vp, C.c_int]),
     }
+    popts = C.POINTER(AdvanceOpts)
     optional = {
-        "tchem_gb_workspace_bytes": (C.c_size_t, [C.POINTER(vp), C.c_int, vp, C.c_int, C.c_int]),
+        "tchem_gb_workspace_bytes": (C.c_size_t, [C.POINTER(vp), C.c_int, C.c_int, popts]),
         "tchem_gb_time_advance": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp,
-                                            vp, vp, C.c_size_t, C.c_int, vp]),
+                                            vp, vp, C.c_size_t, popts, vp]),
+        "tchem_gb_time_advance_hostbuf": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp,
+                                                    vp, vp, popts, vp]),
+        "tchem_gb_device_error": (C.c_int, [vp, vp, C.POINTER(C.c_int32)]),
         "tchem_gb_kforward": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp]),
         "tchem_gb_reaction_rates": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp]),
         "tchem_gb_jacobian": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp]),
+        "tchem_gb_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
         f.restype, f.argtypes = res, args
     for name, (res, args) in optional.items():
-        if hasattr(L, name):
-            f = getattr(L, name)
-            f.restype, f.argtypes = res, args
+        f = getattr(L, name)
+        f.restype, f.argtypes = res, args
     _ = (i32, dbl)
     _lib = L
     return L

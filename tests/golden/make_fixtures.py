@@ -1,0 +1,100 @@
+"""Regenerates the golden fixtures of this directory from a TChem-atm source tree.
+
+Usage: python tests/golden/make_fixtures.py /path/to/TChem-atm
+
+Everything copied is data the reference's own tests and examples use:
+  * mechanism / scenario YAML files (src/examples/runs/atmospheric_chemistry/...),
+  * the mechanism echo files the reference's gtests compare byte-for-byte
+    (src/unit-tests/references/*/kmod.echo),
+  * the CB05CL_AE5 TR-BDF2 golden (src/unit-tests/CB05CL_AE5/references/full_gas.hdf5), read
+    without h5py at its raw data offset (3 x 87 little-endian doubles at byte 2048),
+  * the reference's TR-BDF2 trajectory of the Emission case (Emissions.dat) and the CAMP
+    analytic/solver result tables of the small test mechanisms (*_results.txt).
+Run settings of each case come from the reference's scripts and are recorded in manifest.json.
+"""
+from __future__ import annotations
+
+import json
+import shutil
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+RUNS = "src/examples/runs/atmospheric_chemistry"
+
+
+def main(ref: Path) -> None:
+    mech_dir = HERE / "mechanisms"
+    echo_dir = HERE / "echo"
+    mech_dir.mkdir(exist_ok=True)
+    echo_dir.mkdir(exist_ok=True)
+    copies = {
+        "cb05cl_ae5.yaml": f"{RUNS}/CB05CL_AE5/config_full_gas.yaml",
+        "uci.yaml": f"{RUNS}/uci_e3sm_v3/uci.yaml",
+        "uci_v2.yaml": f"{RUNS}/uci_e3sm_v3/uci_v2.yaml",
+        "uci_v2_test3.yaml": f"{RUNS}/uci_col/uci_v2_test3.yaml",
+        "arrhenius.yaml": f"{RUNS}/Arrhenius/config_arrhenius/config_arrhenius.yaml",
+        "troe.yaml": f"{RUNS}/Troe/config_troe/config_troe.yaml",
+        "photolysis.yaml": f"{RUNS}/Photolysis/config_photolysis.yaml",
+        "cmaq_h2o2.yaml": f"{RUNS}/CMAQ_H2O2/config_cmaq_h2o2.yaml",
+        "cmaq_oh_hno3.yaml": f"{RUNS}/CMAQ_OH_HNO3/config_oh_hno3.yaml",
+        "emission.yaml": f"{RUNS}/Emission/config_emissions.yaml",
+    }
+    for dst, src in copies.items():
+        shutil.copyfile(ref / src, mech_dir / dst)
+    echoes = {
+        "uci.echo": "src/unit-tests/references/reaction_rates/kmod.echo",
+        "uci_v2.echo": "src/unit-tests/references/net_production_rates/kmod.echo",
+        "uci_v2_test3.echo": "src/unit-tests/references/net_production_rates/uci_col/kmod.echo",
+    }
+    for dst, src in echoes.items():
+        shutil.copyfile(ref / src, echo_dir / dst)
+
+    raw = (ref / "src/unit-tests/CB05CL_AE5/references/full_gas.hdf5").read_bytes()
+    golden = np.frombuffer(raw[2048:2048 + 261 * 8], dtype="<f8").reshape(3, 87)
+    np.save(HERE / "cb05cl_ae5_full_gas.npy", golden)
+
+    traj = np.genfromtxt(ref / f"{RUNS}/Emission/Emissions.dat", skip_header=1)
+    np.save(HERE / "emission_trajectory.npy", traj)
+
+    camp = {
+        "arrhenius": ("Arrhenius/rxn_arrhenius_results.txt", 1e-6),
+        "troe": ("Troe/troe_results.txt", 1e-8),
+        "photolysis": ("Photolysis/photolysis_results.txt", 1e-6),
+        "cmaq_h2o2": ("CMAQ_H2O2/CMAQ_H2O2_results.txt", 1e-6),
+        "cmaq_oh_hno3": ("CMAQ_OH_HNO3/CMAQ_OH_HNO3_results.txt", 1e-6),
+        "emission": ("Emission/emission_results.txt", 1e-6),
+    }
+    for name, (src, _) in camp.items():
+        np.save(HERE / f"camp_{name}.npy", np.loadtxt(ref / RUNS / src))
+
+    manifest = {
+        "cb05cl_ae5_full_gas": {
+            "source": "src/unit-tests/CB05CL_AE5/references/full_gas.hdf5",
+            "run": "src/unit-tests/CB05CL_AE5/CMakeLists.txt:22-34",
+            "mechanism": "mechanisms/cb05cl_ae5.yaml",
+            "settings": {"tend": 600, "dtmin": 1e-20, "dtmax": 10, "iters_per_interval": 10, "atol_newton": 1e-18,
+                         "rtol_newton": 1e-8, "max_newton": 20, "intervals": 2, "rtol_time": 1e-4,
+                         "atol_time": 1e-12},
+            "criterion": "compare_tchem.py norm-relative L1/L2/Linf <= 1e-8 (src/unit-tests/scripts/compare_tchem.py)",
+        },
+        "emission_trajectory": {
+            "source": f"{RUNS}/Emission/Emissions.dat",
+            "mechanism": "mechanisms/emission.yaml",
+            "settings": {"tend": 100, "dtmin": 1e-20, "dtmax": 0.1, "iters_per_interval": 10, "rtol_time": 1e-6,
+                         "atol_newton": 1e-18, "rtol_newton": 1e-8, "max_newton": 20, "max_intervals": 200},
+            "run": f"{RUNS}/Emission/runModel.sh",
+        },
+        "camp": {name: {"source": f"{RUNS}/{src}", "mechanism": f"mechanisms/{name}.yaml", "rtol_time": rt,
+                        "settings": {"tend": 100, "dtmin": 1e-20, "dtmax": 0.1, "output_every": 1.0}}
+                 for name, (src, rt) in camp.items()},
+        "echo": {dst: src for dst, src in echoes.items()},
+    }
+    (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1) + "\n")
+    print(f"fixtures written to {HERE}")
+
+
+if __name__ == "__main__":
+    main(Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference"))

@@ -1,0 +1,56 @@
+"""Shared test utilities: fixture loading, the reference's host time loop and its comparison norms."""
+from __future__ import annotations
+
+import json
+from pathlib import Path
+
+import numpy as np
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+
+
+def manifest() -> dict:
+    return json.loads((GOLDEN / "manifest.json").read_text())
+
+
+def mech_path(name: str) -> Path:
+    return GOLDEN / "mechanisms" / name
+
+
+def compare_tchem(test: np.ndarray, ref: np.ndarray) -> float:
+    """Largest of the per-column L1/L2/Linf norms of (test - ref) divided by the column's L2
+    norm (floored at 1e-23), the criterion of src/unit-tests/scripts/compare_tchem.py:8-77."""
+    diff = test - ref
+    den = np.linalg.norm(ref, 2, axis=0)
+    den = np.where(den > 1e-23, den, 1.0)
+    worst = 0.0
+    for ordn in (1, 2, np.inf):
+        e = np.linalg.norm(diff, ordn, axis=0) / den
+        e = np.where(np.all(diff == 0, axis=0), 0.0, e)
+        worst = max(worst, float(e.max()))
+    return worst
+
+
+def rel_error(test: np.ndarray, ref: np.ndarray, floor: float) -> np.ndarray:
+    """Elementwise |test - ref| / max(|ref|, floor)."""
+    return np.abs(test - ref) / np.maximum(np.abs(ref), floor)
+
+
+def host_time_loop(advance, state: np.ndarray, tadv: np.ndarray, tend: float, max_intervals: int, dtmax: float):
+    """The reference box model's host loop (src/examples/TChem_AtmosphericChemistry.cpp:312-352):
+    calls `advance(tadv, state, t) -> (state, t, dt)` until the mean t exceeds 0.9999 tend,
+    carrying t and dt into tadv. Returns the rows (iter, t, dt, state...) of sample 0."""
+    B = state.shape[0]
+    t = np.array(tadv["tbeg"], dtype=np.float64)
+    dt = np.full(B, dtmax)
+    rows = [np.concatenate([[-1, t[0], dt[0]], state[0]])]
+    it = 0
+    tsum = 0.0
+    while it < max_intervals and tsum <= tend * 0.9999:
+        state, t, dt = advance(tadv, state, t)
+        rows.append(np.concatenate([[it, t[0], dt[0]], state[0]]))
+        tadv["tbeg"] = t
+        tadv["dt"] = dt
+        tsum = float(np.mean(t))
+        it += 1
+    return np.array(rows), state

@@ -1,0 +1,300 @@
+"""GPU parity: the engine's CUDA kernels, called through the C ABI, against the CPU oracle.
+
+Tolerances: rate constants, RHS and Jacobian agree to 1e-12 relative (FP64 with a different
+summation order); the plain FP64 time advance agrees with the oracle to 1e-8 per species at the
+end time (relative error floored at 1e-12 = atol_time) and passes the reference's compare_tchem
+criterion at 1e-8; the mixed form agrees with the FP64 oracle to 1e-6 on the same measure.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from helpers import GOLDEN, compare_tchem, host_time_loop, manifest, mech_path, rel_error
+from oracle import Oracle
+from tchem_gb import (AtmosphericChemistry, KineticModel, jacobian, kforward, reaction_rates,
+                      set_scenario_conditions, tadv_to_device, time_advance_array)
+from tchem_gb.generator import MechanismSpec, mechanism_yaml, sample_states
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+ATOL_TIME = 1e-12
+
+
+@pytest.fixture(scope="module")
+def cb05():
+    km = KineticModel.from_string(mechanism_yaml(MechanismSpec()))
+    return km
+
+
+def _dev(a, dtype=None):
+    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype).cuda()
+
+
+def gpu_advance(km, tadv, state, tol_newton, tol_time, t_out=None, form="plain", mech_of_sample=None, stats=False,
+                state_out_alias=False):
+    B = state.shape[0]
+    d_state = _dev(state)
+    d_out = d_state if state_out_alias else d_state.clone()
+    d_t = _dev(tadv["tbeg"] if t_out is None else t_out, torch.float64)
+    d_dt = torch.zeros(B, dtype=torch.float64, device="cuda")
+    d_st = torch.full((B,), -7, dtype=torch.int32, device="cuda")
+    d_stats = torch.zeros(B, 8, dtype=torch.int32, device="cuda") if stats else None
+    mos = None if mech_of_sample is None else _dev(mech_of_sample, torch.int32)
+    AtmosphericChemistry.runDeviceBatch(_dev(tol_newton, torch.float64), _dev(tol_time, torch.float64), None,
+                                        tadv_to_device(tadv), d_state, d_t, d_dt, d_out, km,
+                                        mech_of_sample=mos, status=d_st, stats=d_stats, form=form)
+    torch.cuda.synchronize()
+    assert AtmosphericChemistry.device_error() == 0
+    res = [d_out.cpu().numpy(), d_t.cpu().numpy(), d_dt.cpu().numpy(), d_st.cpu().numpy()]
+    res.append(d_stats.cpu().numpy() if stats else None)
+    return res
+
+
+def generated_case(B, seed=7, horizon=3600.0, km=None):
+    km = km or KineticModel.from_string(mechanism_yaml(MechanismSpec()))
+    state = sample_states(B, km.n_active, seed=seed)
+    tadv = time_advance_array(B, tend=horizon, dt=1e-10, dtmin=1e-10, dtmax=horizon, max_num_newton_iterations=20,
+                              num_time_iterations_per_interval=1_000_000)
+    tol_time = np.tile([ATOL_TIME, 1e-6], (km.n_active, 1))
+    return km, state, tadv, tol_time
+
+
+# --- unit kernels -------------------------------------------------------------------------------
+
+@pytest.mark.parametrize("which", ["generated", "cb05cl_ae5"])
+def test_rate_constants_rhs_jacobian_match_oracle(which):
+    if which == "generated":
+        km = KineticModel.from_string(mechanism_yaml(MechanismSpec()))
+        state = sample_states(64, km.n_active, seed=3)
+    else:
+        km = KineticModel.from_file(mech_path("cb05cl_ae5.yaml"))
+        base = set_scenario_conditions(mech_path("cb05cl_ae5.yaml"), km)
+        rng = np.random.default_rng(1)
+        state = np.repeat(base, 16, axis=0)
+        state[:, 3:3 + km.n_active] *= rng.uniform(0.5, 1.5, size=(16, km.n_active))
+        state[:, 3:3 + km.n_active] += rng.uniform(0, 1e-3, size=(16, km.n_active))
+        state[:, 2] = rng.uniform(260, 310, size=16)
+    o = Oracle([km])
+    d = _dev(state)
+    kf = kforward(km, d).cpu().numpy()
+    om = reaction_rates(km, d).cpu().numpy()
+    J = jacobian(km, d).cpu().numpy()
+    for b in range(state.shape[0]):
+        T, p, x = state[b, 2], state[b, 1], state[b, 3:3 + km.nSpec]
+        np.testing.assert_allclose(kf[b], o.kforward(T, p), rtol=1e-13, atol=0)
+        ro = o.reaction_rates(T, p, x)
+        scale = np.abs(ro).max()
+        assert np.max(np.abs(om[b] - ro)) <= 1e-12 * scale
+        Jo = o.jacobian(T, p, x)
+        assert np.max(np.abs(J[b] - Jo)) <= 1e-12 * np.abs(Jo).max()
+
+
+# --- plain FP64 time advance ----------------------------------------------------------------------
+
+@pytest.fixture(scope="module")
+def cfg1_like():
+    """256 samples of the CB05-shaped 51-species / 156-reaction batch over 3600 s, oracle results."""
+    km, state, tadv, tol_time = generated_case(256)
+    ref = Oracle([km]).time_advance(tadv, state, [1e-18, 1e-8], tol_time)
+    return km, state, tadv, tol_time, ref
+
+
+def test_plain_fp64_matches_oracle_on_cb05_shaped_batch(cfg1_like):
+    km, state, tadv, tol_time, ref = cfg1_like
+    out, t, dt, st, stats = gpu_advance(km, tadv, state, [1e-18, 1e-8], tol_time, stats=True)
+    m = km.n_active
+    assert np.all(st == 0) and np.all(ref[3] == 0)
+    assert np.all(t == 3600.0) and np.all(dt == 0.0)
+    err = rel_error(out[:, 3:3 + m], ref[0][:, 3:3 + m], ATOL_TIME)
+    assert err.max() <= 1e-8, err.max()
+    assert compare_tchem(out[:, 3:3 + m], ref[0][:, 3:3 + m]) <= 1e-8
+    # T, p, rho and constant species pass through unchanged.
+    np.testing.assert_array_equal(out[:, :3], state[:, :3])
+    np.testing.assert_array_equal(out[:, 3 + m:], state[:, 3 + m:])
+    # Same accept/reject and Newton decisions as the oracle on nearly every sample.
+    same = np.all(stats[:, :4] == np.stack([ref[4][f] for f in ("n_steps", "n_rejected", "n_newton_fail",
+                                                                "n_newton_iter")], axis=1), axis=1)
+    assert same.mean() >= 0.98
+
+
+def test_plain_fp64_reproduces_cb05cl_ae5_golden():
+    s = manifest()["cb05cl_ae5_full_gas"]["settings"]
+    km = KineticModel.from_file(mech_path("cb05cl_ae5.yaml"))
+    state = set_scenario_conditions(mech_path("cb05cl_ae5.yaml"), km)
+    tadv = time_advance_array(1, tend=s["tend"], dt=s["dtmin"], dtmin=s["dtmin"], dtmax=s["dtmax"],
+                              max_num_newton_iterations=s["max_newton"],
+                              num_time_iterations_per_interval=s["iters_per_interval"])
+    tol_time = np.tile([s["atol_time"], s["rtol_time"]], (km.n_active, 1))
+
+    def adv(tadv_, state_, t_):
+        out, t, dt, st, _ = gpu_advance(km, tadv_, state_, [s["atol_newton"], s["rtol_newton"]], tol_time,
+                                        t_out=t_, state_out_alias=True)
+        assert np.all(st == 0)
+        return out, t, dt
+
+    rows, _ = host_time_loop(adv, state, tadv, s["tend"], s["intervals"], s["dtmax"])
+    golden = np.load(GOLDEN / "cb05cl_ae5_full_gas.npy")
+    assert compare_tchem(rows, golden) <= 1e-8
+
+
+def test_plain_fp64_reproduces_reference_emission_trajectory():
+    s = manifest()["emission_trajectory"]["settings"]
+    km = KineticModel.from_file(mech_path("emission.yaml"))
+    state = set_scenario_conditions(mech_path("emission.yaml"), km)
+    tadv = time_advance_array(1, tend=s["tend"], dt=s["dtmin"], dtmin=s["dtmin"], dtmax=s["dtmax"],
+                              max_num_newton_iterations=s["max_newton"],
+                              num_time_iterations_per_interval=s["iters_per_interval"])
+    tol_time = np.tile([1e-12, s["rtol_time"]], (km.n_active, 1))
+
+    def adv(tadv_, state_, t_):
+        out, t, dt, st, _ = gpu_advance(km, tadv_, state_, [s["atol_newton"], s["rtol_newton"]], tol_time, t_out=t_)
+        return out, t, dt
+
+    rows, _ = host_time_loop(adv, state, tadv, s["tend"], s["max_intervals"], s["dtmax"])
+    ref = np.load(GOLDEN / "emission_trajectory.npy")
+    assert rows.shape[0] == ref.shape[0]
+    assert rel_error(rows[:, 1:8], ref[:, 1:8], 1e-300).max() < 1e-10
+
+
+def test_edge_cases_skip_negative_dt_failure_and_aliasing(cb05):
+    km, state, tadv, tol_time = generated_case(6, seed=9, horizon=60.0, km=cb05)
+    t_in = np.array([0.0, 60.0, 0.0, 0.0, 0.0, 75.0])  # samples 1 and 5 are already at/after t_end
+    tadv["dt"][2] = -1.0                                # negative dt_in
+    ref = Oracle([km]).time_advance(tadv, state, [1e-18, 1e-8], tol_time, t_out=t_in)
+    out, t, dt, st, _ = gpu_advance(km, tadv, state, [1e-18, 1e-8], tol_time, t_out=t_in)
+    np.testing.assert_array_equal(st, ref[3])
+    assert list(st) == [0, 2, 3, 0, 0, 2]
+    for b in (1, 2, 5):
+        np.testing.assert_array_equal(out[b], state[b])
+    assert t[1] == 60.0 and t[5] == 75.0 and t[2] == 0.0
+    m = km.n_active
+    assert rel_error(out[[0, 3, 4], 3:3 + m], ref[0][[0, 3, 4], 3:3 + m], ATOL_TIME).max() <= 1e-8
+    # In place (state_out is state) gives the same numbers.
+    out2, *_ = gpu_advance(km, tadv, state, [1e-18, 1e-8], tol_time, t_out=t_in, state_out_alias=True)
+    np.testing.assert_array_equal(out2, out)
+    # Newton failure convention.
+    out3, t3, dt3, st3, stats3 = gpu_advance(km, generated_case(3, km=cb05)[2], state[:3], [-1.0, 0.0], tol_time,
+                                             stats=True)
+    assert np.all(st3 == 1) and np.all(t3 == 3600.0) and np.all(dt3 == -1.0)
+    assert np.all(out3[:, 3:3 + m] == 0.0) and np.all(stats3[:, 2] == 4)
+
+
+def test_empty_batch_and_host_buffer_entry_point(cb05):
+    km, state, tadv, tol_time = generated_case(8, seed=21, horizon=120.0, km=cb05)
+    out, t, dt, st, _ = gpu_advance(km, tadv, state, [1e-18, 1e-8], tol_time)
+    h_out, h_t, h_dt, h_st, h_stats = AtmosphericChemistry.runHostBatch([1e-18, 1e-8], tol_time, tadv, state,
+                                                                        tadv["tbeg"], km, with_stats=True)
+    np.testing.assert_array_equal(h_out, out)
+    np.testing.assert_array_equal(h_t, t)
+    np.testing.assert_array_equal(h_st, st)
+    assert h_stats["n_steps"].min() > 0
+    e = gpu_advance(km, tadv[:0], state[:0], [1e-18, 1e-8], tol_time)
+    assert e[0].shape == (0, state.shape[1])
+
+
+def test_per_sample_mechanisms_match_oracle():
+    """kmcds overload: day/night variants of the 51-species mechanism (one structure, one launch)
+    plus a second, smaller mechanism (its own launch), selected per sample."""
+    day = KineticModel.from_string(mechanism_yaml(MechanismSpec()))
+    night = KineticModel.from_string(mechanism_yaml(MechanismSpec(), night=True))
+    small = KineticModel.from_string(mechanism_yaml(MechanismSpec(n_species=20, n_reactions=60, seed=99)))
+    mechs = [day, night, small]
+    B = 48
+    dim = day.state_dim
+    state = np.zeros((B, dim))
+    mos = np.array([i % 3 for i in range(B)], dtype=np.int32)
+    big = sample_states(B, day.n_active, seed=4)
+    sm = sample_states(B, small.n_active, seed=5)
+    for b in range(B):
+        if mos[b] == 2:
+            state[b, :3 + small.nSpec] = sm[b]
+        else:
+            state[b] = big[b]
+    tadv = time_advance_array(B, tend=600.0, dt=1e-10, dtmin=1e-10, dtmax=600.0, max_num_newton_iterations=20,
+                              num_time_iterations_per_interval=1_000_000)
+    tol_time = np.tile([ATOL_TIME, 1e-6], (day.n_active, 1))
+    ref = Oracle(mechs).time_advance(tadv, state, [1e-18, 1e-8], tol_time, mech_of_sample=mos)
+    out, t, dt, st, _ = gpu_advance(mechs, tadv, state, [1e-18, 1e-8], tol_time, mech_of_sample=mos)
+    assert np.all(st == 0) and np.all(ref[3] == 0)
+    for b in range(B):
+        n = (small if mos[b] == 2 else day).n_active
+        e = rel_error(out[b, 3:3 + n], ref[0][b, 3:3 + n], ATOL_TIME).max()
+        assert e <= 1e-8, (b, e)
+    # A sample naming no mechanism of the call is flagged, not computed.
+    bad = mos.copy()
+    bad[5] = 7
+    *_, st_bad, _ = gpu_advance(mechs, tadv, state, [1e-18, 1e-8], tol_time, mech_of_sample=bad)
+    assert st_bad[5] == 6 and np.all(np.delete(st_bad, 5) == 0)
+
+
+# --- mixed-precision form ---------------------------------------------------------------------------
+
+def test_mixed_matches_fp64_oracle_on_cb05_shaped_batch(cfg1_like):
+    km, state, tadv, tol_time, ref = cfg1_like
+    out, t, dt, st, stats = gpu_advance(km, tadv, state, [1e-18, 1e-8], tol_time, form="mixed", stats=True)
+    m = km.n_active
+    assert np.all(st == 0)
+    assert np.all(t == 3600.0) and np.all(dt == 0.0)
+    err = rel_error(out[:, 3:3 + m], ref[0][:, 3:3 + m], ATOL_TIME)
+    assert err.max() <= 1e-6, err.max()
+    np.testing.assert_array_equal(out[:, :3], state[:, :3])
+    # The FP32 LU does not change the step-size sequence much: mean steps within 1 %.
+    assert abs(stats[:, 0].mean() / ref[4]["n_steps"].mean() - 1.0) < 0.01
+
+
+@pytest.mark.parametrize("tps", [0, 32])
+def test_mixed_threads_per_sample_shapes_agree(cb05, tps):
+    km, state, tadv, tol_time = generated_case(24, seed=31, horizon=600.0, km=cb05)
+    ref = Oracle([km]).time_advance(tadv, state, [1e-18, 1e-8], tol_time)
+    d_state = _dev(state)
+    d_out = d_state.clone()
+    d_t = torch.zeros(24, dtype=torch.float64, device="cuda")
+    d_dt = torch.zeros_like(d_t)
+    st = AtmosphericChemistry.runDeviceBatch(_dev([1e-18, 1e-8]), _dev(tol_time), None, tadv_to_device(tadv), d_state,
+                                             d_t, d_dt, d_out, km, form="mixed", threads_per_sample=tps)
+    torch.cuda.synchronize()
+    assert int((st != 0).sum()) == 0
+    m = km.n_active
+    err = rel_error(d_out.cpu().numpy()[:, 3:3 + m], ref[0][:, 3:3 + m], ATOL_TIME)
+    assert err.max() <= 1e-6
+
+
+def test_mixed_per_sample_mechanisms_and_edge_cases():
+    day = KineticModel.from_string(mechanism_yaml(MechanismSpec()))
+    night = KineticModel.from_string(mechanism_yaml(MechanismSpec(), night=True))
+    small = KineticModel.from_string(mechanism_yaml(MechanismSpec(n_species=20, n_reactions=60, seed=99)))
+    mechs = [day, night, small]
+    B = 30
+    state = np.zeros((B, day.state_dim))
+    mos = np.array([i % 3 for i in range(B)], dtype=np.int32)
+    big = sample_states(B, day.n_active, seed=14)
+    sm = sample_states(B, small.n_active, seed=15)
+    for b in range(B):
+        if mos[b] == 2:
+            state[b, :3 + small.nSpec] = sm[b]
+        else:
+            state[b] = big[b]
+    tadv = time_advance_array(B, tend=600.0, dt=1e-10, dtmin=1e-10, dtmax=600.0, max_num_newton_iterations=20,
+                              num_time_iterations_per_interval=1_000_000)
+    t_in = np.zeros(B)
+    t_in[4] = 600.0         # skipped
+    tadv["dt"][7] = -1.0    # negative dt_in
+    tol_time = np.tile([ATOL_TIME, 1e-6], (day.n_active, 1))
+    ref = Oracle(mechs).time_advance(tadv, state, [1e-18, 1e-8], tol_time, t_out=t_in, mech_of_sample=mos)
+    out, t, dt, st, _ = gpu_advance(mechs, tadv, state, [1e-18, 1e-8], tol_time, t_out=t_in, form="mixed",
+                                    mech_of_sample=mos)
+    np.testing.assert_array_equal(st, ref[3])
+    assert st[4] == 2 and st[7] == 3
+    np.testing.assert_array_equal(out[[4, 7]], state[[4, 7]])
+    for b in range(B):
+        if b in (4, 7):
+            continue
+        n = (small if mos[b] == 2 else day).n_active
+        assert rel_error(out[b, 3:3 + n], ref[0][b, 3:3 + n], ATOL_TIME).max() <= 1e-6, b
+    # Newton failure convention in the mixed form too.
+    out3, t3, dt3, st3, _ = gpu_advance(day, tadv[:3], big[:3], [-1.0, 0.0], tol_time, form="mixed")
+    assert np.all(st3 == 1) and np.all(t3 == 600.0) and np.all(dt3 == -1.0)
+    assert np.all(out3[:, 3:3 + day.n_active] == 0.0)
