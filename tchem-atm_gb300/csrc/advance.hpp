@@ -11,6 +11,14 @@ namespace tchem_gb {
 constexpr int kMaxMechs = 64;       // mechanisms per time-advance call
 constexpr int kMaxGroupSlots = 8;   // structure-compatible mechanisms sharing one launch
 
+// Byte offsets of the sections of one warp's shared-memory region (mixed form). Kept in the
+// kernel parameters (constant bank) so section addresses cost no registers.
+struct MixedLayout {
+  uint32_t warp_bytes;
+  uint32_t x, keff, q, x32, keff32, d32, ustage, lrow, pinv, piv, ybuf, vec, stats, item;
+  int32_t LDU, LDL;
+};
+
 struct AdvanceParams {
   MechDev mech;                                 // tables of the group (shared structure)
   const double* rate_param[kMaxGroupSlots];     // per slot: [R][8] rate parameters
@@ -36,6 +44,7 @@ struct AdvanceParams {
   int32_t matrix_in_smem;
   uint32_t warp_smem_bytes;
   int32_t* error_word;                          // device-side error report (bounded waits)
+  MixedLayout ml;                               // mixed form only
 };
 
 }  // namespace tchem_gb

@@ -63,6 +63,7 @@ struct GroupPlan {
   size_t gmat_offset = 0;
   size_t gmat_elems_per_warp = 0;
   int threads_per_sample = 32;
+  MixedLayout ml{};
 };
 
 struct Plan {
@@ -111,6 +112,7 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
   }
   const DeviceInfo info = device_info(dev);
   for (auto& g : plan.groups) {
+    if (o.form == TCHEM_GB_FORM_MIXED) g.dev = dts[g.mechs[0]]->dev_x;  // sliced-ELL tables
     const MechLayout& L = g.dev.L;
     plan.m_max = std::max(plan.m_max, L.m);
     g.form = o.form;
@@ -121,6 +123,7 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
       g.grid = mc.grid;
       g.smem = mc.smem;
       g.threads_per_sample = mc.threads_per_sample;
+      g.ml = mc.ml;
       g.matrix_in_smem = true;
       g.lda = L.m;
       continue;
@@ -322,6 +325,7 @@ int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const 
     P.matrix_in_smem = gp.matrix_in_smem ? 1 : 0;
     P.warp_smem_bytes = gp.warp_smem;
     P.error_word = error_word;
+    P.ml = gp.ml;
     if (gp.form == TCHEM_GB_FORM_MIXED)
       e = launch_trbdf2_mixed(P, gp.dev.L, gp.grid, gp.warps_per_block, gp.smem, gp.threads_per_sample, stream);
     else

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -18,6 +19,51 @@ size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 template <typename T>
 void put(std::vector<unsigned char>& blob, int32_t off, const std::vector<T>& v) {
   if (!v.empty()) std::memcpy(blob.data() + off, v.data(), v.size() * sizeof(T));
+}
+
+// Sliced-ELL layout of variable-length lists: items sorted by length (descending, stable), 32 per
+// slice; slice s holds cnt[s] entry rows of 32 lanes starting at entry off[s]; short lists are
+// padded with (dummy, 0). item[s * 32 + lane] is the item id, or -1 for a padding lane.
+struct Sliced {
+  std::vector<int32_t> item, cnt, off;
+  std::vector<int16_t> idx;
+  std::vector<double> val;
+};
+
+Sliced make_slices(const std::vector<std::vector<std::pair<int, double>>>& lists, const std::vector<int32_t>& ids,
+                   int16_t dummy) {
+  const int n = static_cast<int>(lists.size());
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return lists[a].size() > lists[b].size(); });
+  Sliced s;
+  const int nsl = (n + 31) / 32;
+  int32_t e = 0;
+  for (int sl = 0; sl < nsl; ++sl) {
+    int c = 0;
+    for (int l = 0; l < 32; ++l) {
+      const int k = sl * 32 + l;
+      s.item.push_back(k < n ? ids[order[k]] : -1);
+      if (k < n) c = std::max(c, static_cast<int>(lists[order[k]].size()));
+    }
+    s.cnt.push_back(c);
+    s.off.push_back(e);
+    for (int r = 0; r < c; ++r) {
+      for (int l = 0; l < 32; ++l) {
+        const int k = sl * 32 + l;
+        if (k < n && r < static_cast<int>(lists[order[k]].size())) {
+          s.idx.push_back(static_cast<int16_t>(lists[order[k]][r].first));
+          s.val.push_back(lists[order[k]][r].second);
+        } else {
+          s.idx.push_back(dummy);
+          s.val.push_back(0.0);
+        }
+      }
+    }
+    e += 32 * c;
+  }
+  return s;
 }
 
 }  // namespace
@@ -168,6 +214,59 @@ HostTables build_host_tables(const KineticModel& km) {
   put(ht.blob, L.off_jc_nu, jc_nu);
   put(ht.blob, L.off_jc_nu32, jc_nu32);
 
+  // Mixed-form blob: the same rate-of-progress program plus sliced-ELL programs.
+  {
+    std::vector<std::vector<std::pair<int, double>>> jlists;
+    std::vector<int32_t> jids;
+    for (const auto& kv : jac) {
+      jids.push_back((kv.first.first << 16) | kv.first.second);
+      jlists.push_back(kv.second);
+    }
+    std::vector<int32_t> wids(m);
+    for (int k = 0; k < m; ++k) wids[k] = k;
+    const Sliced js = make_slices(jlists, jids, static_cast<int16_t>(L.NF));
+    const Sliced ws = make_slices(per_species, wids, static_cast<int16_t>(R));
+    std::vector<float> jse_nu32(js.val.begin(), js.val.end());
+    MechLayout& X = ht.Lx;
+    X = L;
+    X.NJS = static_cast<int32_t>(js.cnt.size());
+    X.NJE = static_cast<int32_t>(js.idx.size());
+    X.NWS = static_cast<int32_t>(ws.cnt.size());
+    X.NWE = static_cast<int32_t>(ws.idx.size());
+    size_t o = 0;
+    auto sx = [&](size_t bytes) { const int32_t r = static_cast<int32_t>(o); o = align16(o + bytes); return r; };
+    X.off_emis = sx(sizeof(double) * m);
+    X.off_rf_ptr = sx(sizeof(int32_t) * (R + 1));
+    X.off_wse_nu = sx(sizeof(double) * ws.val.size());
+    X.off_js_rc = sx(sizeof(int32_t) * js.item.size());
+    X.off_js_cnt = sx(sizeof(int32_t) * js.cnt.size());
+    X.off_js_off = sx(sizeof(int32_t) * js.off.size());
+    X.off_jse_nu32 = sx(sizeof(float) * jse_nu32.size());
+    X.off_ws_sp = sx(sizeof(int32_t) * ws.item.size());
+    X.off_ws_cnt = sx(sizeof(int32_t) * ws.cnt.size());
+    X.off_ws_off = sx(sizeof(int32_t) * ws.off.size());
+    X.off_rf_sp = sx(sizeof(int16_t) * rf_sp.size());
+    X.off_jse_f = sx(sizeof(int16_t) * js.idx.size());
+    X.off_wse_r = sx(sizeof(int16_t) * ws.idx.size());
+    // CSR sections are not part of the mixed blob
+    X.off_pr_ptr = X.off_pr_r = X.off_pr_nu = X.off_jz_rc = X.off_jz_ptr = X.off_jc_f = X.off_jc_nu = X.off_jc_nu32 = -1;
+    X.blob_bytes = static_cast<int32_t>(align16(o));
+    ht.blob_x.assign(X.blob_bytes, 0);
+    put(ht.blob_x, X.off_emis, emis);
+    put(ht.blob_x, X.off_rf_ptr, rf_ptr);
+    put(ht.blob_x, X.off_rf_sp, rf_sp);
+    put(ht.blob_x, X.off_js_rc, js.item);
+    put(ht.blob_x, X.off_js_cnt, js.cnt);
+    put(ht.blob_x, X.off_js_off, js.off);
+    put(ht.blob_x, X.off_jse_f, js.idx);
+    put(ht.blob_x, X.off_jse_nu32, jse_nu32);
+    put(ht.blob_x, X.off_ws_sp, ws.item);
+    put(ht.blob_x, X.off_ws_cnt, ws.cnt);
+    put(ht.blob_x, X.off_ws_off, ws.off);
+    put(ht.blob_x, X.off_wse_r, ws.idx);
+    put(ht.blob_x, X.off_wse_nu, ws.val);
+  }
+
   // Structural signature: everything except the rate parameters.
   auto mix = [&](int64_t v) { ht.signature.push_back(v); };
   mix(m); mix(n); mix(R);
@@ -185,6 +284,7 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   size_t off = 0;
   auto sec = [&](size_t bytes) { const size_t o = off; off = (off + bytes + 255) & ~size_t(255); return o; };
   const size_t o_blob = sec(L.blob_bytes);
+  const size_t o_blob_x = sec(ht.Lx.blob_bytes);
   const size_t o_type = sec(sizeof(int32_t) * R);
   const size_t o_param = sec(sizeof(double) * R * 8);
   const size_t o_conv = sec(sizeof(int32_t) * R);
@@ -192,6 +292,7 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   const size_t o_cfi = sec(sizeof(int32_t) * std::max<size_t>(1, ht.cf_idx.size()));
   std::vector<unsigned char> host(off, 0);
   std::memcpy(host.data() + o_blob, ht.blob.data(), ht.blob.size());
+  std::memcpy(host.data() + o_blob_x, ht.blob_x.data(), ht.blob_x.size());
   std::memcpy(host.data() + o_type, ht.rate_type.data(), sizeof(int32_t) * R);
   std::memcpy(host.data() + o_param, ht.rate_param.data(), sizeof(double) * R * 8);
   std::memcpy(host.data() + o_conv, ht.conv_exp.data(), sizeof(int32_t) * R);
@@ -225,6 +326,9 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   t->dev.cf_ptr = reinterpret_cast<const int32_t*>(b + o_cfp);
   t->dev.cf_idx = reinterpret_cast<const int32_t*>(b + o_cfi);
   t->dev.conv_ppm = CONV_PPM;
+  t->dev_x = t->dev;
+  t->dev_x.L = ht.Lx;
+  t->dev_x.blob = b + o_blob_x;
   return t;
 }
 

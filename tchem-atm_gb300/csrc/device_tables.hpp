@@ -36,6 +36,13 @@ struct MechLayout {
   int32_t off_emis;                         // double[m]
   int32_t blob_bytes;                       // multiple of 16
   int32_t max_factors;                      // max factor slots of one reaction
+  // Sliced-ELL programs of the mixed form (blob_x): items sorted by entry count, 32 per slice,
+  // entries stored [slice][entry][lane] and padded within the slice with a dummy index whose
+  // value is 0 (d32[NF] for the Jacobian, q[R] for the net production), so every lane of a
+  // slice runs the same trip count with independent loads.
+  int32_t NJS, NJE, NWS, NWE;
+  int32_t off_js_rc, off_js_cnt, off_js_off, off_jse_f, off_jse_nu32;  // Jacobian nonzeros
+  int32_t off_ws_sp, off_ws_cnt, off_ws_off, off_wse_r, off_wse_nu;    // net production per species
 };
 
 // Device pointers of one mechanism on one device (passed by value to kernels).
@@ -52,8 +59,10 @@ struct MechDev {
 
 // Host-side packed tables, built from a parsed kinetic model.
 struct HostTables {
-  MechLayout L{};
+  MechLayout L{};                  // plain form (CSR programs)
   std::vector<unsigned char> blob;
+  MechLayout Lx{};                 // mixed form (sliced-ELL programs)
+  std::vector<unsigned char> blob_x;
   std::vector<int32_t> rate_type, conv_exp, cf_ptr, cf_idx;
   std::vector<double> rate_param;
   // Structural signature: mechanisms with equal signatures share one kernel launch.
@@ -66,7 +75,8 @@ HostTables build_host_tables(const KineticModel& km);
 
 struct DeviceTables {
   int device = -1;
-  MechDev dev{};
+  MechDev dev{};    // plain-form tables
+  MechDev dev_x{};  // mixed-form tables (same rate parameters, sliced-ELL blob)
   void* allocation = nullptr;
 };
 

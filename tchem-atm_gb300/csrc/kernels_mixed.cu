@@ -58,13 +58,15 @@ MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_cou
     throw std::domain_error("mixed form: threads_per_sample must be 0 or 32");
   const Variant* best = pick(L);
   if (!best) throw std::domain_error("mixed form: mechanisms with more than 64 active species are not supported");
-  const size_t gbytes = mixed::group_smem_bytes(L, best->MC);
+  const MixedLayout ml = mixed::make_layout(L, best->MC);
+  const size_t gbytes = ml.warp_bytes;
   const size_t avail = static_cast<size_t>(max_smem_optin) - 16 - L.blob_bytes;
   const int warps = static_cast<int>(std::min<size_t>(kMaxWarps, avail / gbytes));
   if (warps < 1) throw std::domain_error("mixed form: shared-memory working set too large");
   MixedConfig mc;
   mc.kernel = best->kernel;
   mc.threads_per_sample = 32;
+  mc.ml = ml;
   mc.warps_per_block = warps;
   mc.smem = 16 + L.blob_bytes + warps * gbytes;
   cudaFuncSetAttribute(mc.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(mc.smem));

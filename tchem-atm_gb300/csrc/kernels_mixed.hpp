@@ -14,6 +14,7 @@ struct MixedConfig {
   int grid = 0;
   size_t smem = 0;
   int threads_per_sample = 32;
+  MixedLayout ml{};
 };
 
 MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch);

@@ -17,6 +17,10 @@
 // back substitution walks the stored U rows. The right-hand side, the Newton residual, the state,
 // the local-error estimate and the step-size control are FP64; the Jacobian, the LU and the
 // triangular solves are FP32, and Newton iterates to the FP64 fixed point.
+//
+// Registers hold the matrix rows and the Newton iterate; everything touched once per step (the
+// FP64 stage vectors, tolerances, counters) lives in shared memory at offsets taken from the kernel
+// parameters, so no register is spent on addresses.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -34,60 +38,34 @@ namespace mixed {
 // 16-byte row loads of 8 consecutive lanes hit distinct banks and the column walk of the back
 // substitution (stride LDU - 1, odd) is conflict-free.
 __host__ __device__ constexpr int ldu_for(int MC) { return (MC % 8 == 4) ? MC : MC + 4; }
-// Row stride of the L factor: odd, so the per-lane column accesses are conflict-free.
-__host__ __device__ inline int ldl_for(int m) { return m | 1; }
 
-__host__ __device__ inline size_t up16(size_t b) { return (b + 15) & ~size_t(15); }
+// Stage vectors kept in shared memory (FP64, [kVec][m]).
+enum Vec { V_FN = 0, V_FG = 1, V_F1 = 2, V_ATOL = 3, V_RTOL = 4, V_EST = 5, kVec = 6 };
+// Work counters kept in shared memory, in tchem_gb_sample_stats order.
+enum Stat { S_STEPS = 0, S_REJ = 1, S_NFAIL = 2, S_NEWTON = 3, S_LU = 4, S_SOLVE = 5, S_RHS = 6, S_JAC = 7 };
 
-struct MixedSmem {
-  double* x;      // [m] FP64 iterate for the RHS gathers
-  double* keff;   // [R]
-  double* q;      // [R]
-  float* x32;     // [m]
-  float* keff32;  // [R]
-  float* d32;     // [NF]
-  float* ustage;  // [m][LDU] Newton-matrix staging, then U rows in step order: U(k, k+1+j) at [k][j]
-  float* lrow;    // [m][LDL] multiplier of row r at step k
-  float* pinv;    // [m] 1 / pivot of step k
-  int* piv;       // [m] pivot row of step k
-  float* ybuf;    // [m] forward-substitution values in step order
-  int* item;      // [4] work-queue item
-};
-
-__host__ __device__ inline size_t group_smem_bytes(const MechLayout& L, int MC) {
-  const int LDU = ldu_for(MC), LDL = ldl_for(L.m);
-  size_t b = 0;
-  b += up16(sizeof(double) * L.m);
-  b += up16(sizeof(double) * L.R) * 2;
-  b += up16(sizeof(float) * L.m);
-  b += up16(sizeof(float) * L.R);
-  b += up16(sizeof(float) * L.NF);
-  b += up16(sizeof(float) * static_cast<size_t>(L.m) * LDU);
-  b += up16(sizeof(float) * static_cast<size_t>(L.m) * LDL);
-  b += up16(sizeof(float) * L.m);
-  b += up16(sizeof(int) * L.m);
-  b += up16(sizeof(float) * L.m);
-  b += up16(sizeof(int) * 4);
-  return b;
-}
-
-__device__ inline MixedSmem carve(unsigned char* p, const MechLayout& L, int MC) {
-  const int LDU = ldu_for(MC), LDL = ldl_for(L.m);
-  MixedSmem s;
-  auto take = [&](size_t bytes) { unsigned char* r = p; p += up16(bytes); return r; };
-  s.x = reinterpret_cast<double*>(take(sizeof(double) * L.m));
-  s.keff = reinterpret_cast<double*>(take(sizeof(double) * L.R));
-  s.q = reinterpret_cast<double*>(take(sizeof(double) * L.R));
-  s.x32 = reinterpret_cast<float*>(take(sizeof(float) * L.m));
-  s.keff32 = reinterpret_cast<float*>(take(sizeof(float) * L.R));
-  s.d32 = reinterpret_cast<float*>(take(sizeof(float) * L.NF));
-  s.ustage = reinterpret_cast<float*>(take(sizeof(float) * static_cast<size_t>(L.m) * LDU));
-  s.lrow = reinterpret_cast<float*>(take(sizeof(float) * static_cast<size_t>(L.m) * LDL));
-  s.pinv = reinterpret_cast<float*>(take(sizeof(float) * L.m));
-  s.piv = reinterpret_cast<int*>(take(sizeof(int) * L.m));
-  s.ybuf = reinterpret_cast<float*>(take(sizeof(float) * L.m));
-  s.item = reinterpret_cast<int*>(take(sizeof(int) * 4));
-  return s;
+inline MixedLayout make_layout(const MechLayout& L, int MC) {
+  auto up16 = [](size_t b) { return static_cast<uint32_t>((b + 15) & ~size_t(15)); };
+  MixedLayout ml{};
+  ml.LDU = ldu_for(MC);
+  ml.LDL = L.m | 1;
+  uint32_t o = 0;
+  ml.x = o; o += up16(sizeof(double) * L.m);
+  ml.keff = o; o += up16(sizeof(double) * L.R);
+  ml.q = o; o += up16(sizeof(double) * (L.R + 1));  // q[R] = 0 is the padding target
+  ml.vec = o; o += up16(sizeof(double) * kVec * L.m);
+  ml.x32 = o; o += up16(sizeof(float) * L.m);
+  ml.keff32 = o; o += up16(sizeof(float) * L.R);
+  ml.d32 = o; o += up16(sizeof(float) * (L.NF + 1));  // d32[NF] = 0 is the padding target
+  ml.ustage = o; o += up16(sizeof(float) * static_cast<size_t>(L.m) * ml.LDU);
+  ml.lrow = o; o += up16(sizeof(float) * static_cast<size_t>(L.m) * ml.LDL);
+  ml.pinv = o; o += up16(sizeof(float) * L.m);
+  ml.piv = o; o += up16(sizeof(int) * L.m);
+  ml.ybuf = o; o += up16(sizeof(float) * L.m);
+  ml.stats = o; o += up16(sizeof(int) * 8);
+  ml.item = o; o += up16(sizeof(int) * 4);
+  ml.warp_bytes = o;
+  return ml;
 }
 
 template <int MC, int RPT>
@@ -95,82 +73,156 @@ struct Solver {
   static_assert(MC % 4 == 0, "MC must be a multiple of 4");
   static constexpr int LDU = ldu_for(MC);
 
-  SmemTables T;
-  MixedSmem M;
-  int m, R, NZ, lane, LDL;
-  tchem_gb_sample_stats st;
+  const AdvanceParams& P;
+  const unsigned char* tb;  // staged tables
+  unsigned char* wb;        // this warp's region
+  int lane;
 
   float A[RPT][MC];  // active rows, shifted: register j holds column k + j at step k
   int step[RPT];     // step at which the row became the pivot (INT_MAX while active)
 
+  __device__ __forceinline__ int m() const { return P.mech.L.m; }
   __device__ __forceinline__ int row(int s) const { return lane + 32 * s; }
+  template <typename Tp>
+  __device__ __forceinline__ Tp* w(uint32_t off) const { return reinterpret_cast<Tp*>(wb + off); }
+  template <typename Tp>
+  __device__ __forceinline__ const Tp* t(int32_t off) const { return reinterpret_cast<const Tp*>(tb + off); }
+  __device__ __forceinline__ double& vec(int v, int i) const { return w<double>(P.ml.vec)[v * m() + i]; }
+  __device__ __forceinline__ void count(int which) const {
+    if (lane == 0) ++w<int>(P.ml.stats)[which];
+  }
 
   // ---- FP64 right-hand side: src/core/impl/TChem_Impl_ReactionRatesAerosol.hpp:80-138 -----
+  // f = omega(y), y in registers (by row); f returned by row.
   __device__ __forceinline__ void rhs(const double (&y)[RPT], double (&f)[RPT]) {
+    const MechLayout& L = P.mech.L;
+    double* x = w<double>(P.ml.x);
+    double* q = w<double>(P.ml.q);
+    const double* keff = w<double>(P.ml.keff);
 #pragma unroll
     for (int s = 0; s < RPT; ++s)
-      if (row(s) < m) M.x[row(s)] = y[s];
+      if (row(s) < L.m) x[row(s)] = y[s];
     __syncwarp();
-    for (int r = lane; r < R; r += 32) {
-      double q = M.keff[r];
-      for (int g = T.rf_ptr[r]; g < T.rf_ptr[r + 1]; ++g) q *= M.x[T.rf_sp[g]];
-      M.q[r] = q;
+    const int32_t* rf_ptr = t<int32_t>(L.off_rf_ptr);
+    const int16_t* rf_sp = t<int16_t>(L.off_rf_sp);
+#pragma unroll 2
+    for (int r = lane; r < L.R; r += 32) {
+      const int g0 = rf_ptr[r], g1 = rf_ptr[r + 1];
+      double qq = keff[r];
+      if (g1 > g0) qq *= x[rf_sp[g0]];
+      if (g1 > g0 + 1) qq *= x[rf_sp[g0 + 1]];
+      for (int g = g0 + 2; g < g1; ++g) qq *= x[rf_sp[g]];
+      q[r] = qq;
+    }
+    __syncwarp();
+    // net production over species slices (sliced ELL); results staged in x by species
+    const int32_t* ws_sp = t<int32_t>(L.off_ws_sp);
+    const int32_t* ws_cnt = t<int32_t>(L.off_ws_cnt);
+    const int32_t* ws_off = t<int32_t>(L.off_ws_off);
+    const int16_t* wse_r = t<int16_t>(L.off_wse_r);
+    const double* wse_nu = t<double>(L.off_wse_nu);
+    const double* emis = t<double>(L.off_emis);
+#pragma unroll 2
+    for (int sl = 0; sl < L.NWS; ++sl) {
+      const int sp = ws_sp[sl * 32 + lane];
+      const int cnt = ws_cnt[sl];
+      const int base = ws_off[sl] + lane;
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      int c = 0;
+      for (; c + 4 <= cnt; c += 4) {
+        const int e = base + 32 * c;
+        const int r0 = wse_r[e], r1 = wse_r[e + 32], r2 = wse_r[e + 64], r3 = wse_r[e + 96];
+        a0 += wse_nu[e] * q[r0];
+        a1 += wse_nu[e + 32] * q[r1];
+        a2 += wse_nu[e + 64] * q[r2];
+        a3 += wse_nu[e + 96] * q[r3];
+      }
+      for (; c < cnt; ++c) a0 += wse_nu[base + 32 * c] * q[wse_r[base + 32 * c]];
+      if (sp >= 0) x[sp] = emis[sp] + ((a0 + a1) + (a2 + a3));
     }
     __syncwarp();
 #pragma unroll
-    for (int s = 0; s < RPT; ++s) {
-      const int i = row(s);
-      double acc = 0.0;
-      if (i < m) {
-        acc = T.emis[i];
-        for (int e = T.pr_ptr[i]; e < T.pr_ptr[i + 1]; ++e) acc += T.pr_nu[e] * M.q[T.pr_r[e]];
-      }
-      f[s] = acc;
-    }
+    for (int s = 0; s < RPT; ++s) f[s] = row(s) < L.m ? x[row(s)] : 0.0;
     __syncwarp();
-    ++st.n_rhs;
+    count(S_RHS);
   }
 
   // ---- FP32 Newton matrix A = I - coef J(y) into registers -----------------------------
   __device__ __forceinline__ void newton_matrix(const double (&y)[RPT], double coef) {
+    const MechLayout& L = P.mech.L;
+    const int mm = L.m;
+    float* x32 = w<float>(P.ml.x32);
+    float* d32 = w<float>(P.ml.d32);
+    float* stage = w<float>(P.ml.ustage);
+    const float* keff32 = w<float>(P.ml.keff32);
 #pragma unroll
     for (int s = 0; s < RPT; ++s)
-      if (row(s) < m) M.x32[row(s)] = static_cast<float>(y[s]);
+      if (row(s) < mm) x32[row(s)] = static_cast<float>(y[s]);
     // identity rows into the staging matrix (columns >= m stay 0)
-    for (int e = lane; e < m * (LDU / 4); e += 32) {
+    for (int e = lane; e < mm * (LDU / 4); e += 32) {
       const int i = e / (LDU / 4), j4 = (e - i * (LDU / 4)) * 4;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       if (i == j4) v.x = 1.f;
       if (i == j4 + 1) v.y = 1.f;
       if (i == j4 + 2) v.z = 1.f;
       if (i == j4 + 3) v.w = 1.f;
-      reinterpret_cast<float4*>(M.ustage + static_cast<size_t>(i) * LDU)[j4 / 4] = v;
+      reinterpret_cast<float4*>(stage + i * LDU)[j4 / 4] = v;
     }
     __syncwarp();
-    for (int r = lane; r < R; r += 32) {
-      const int f0 = T.rf_ptr[r], f1 = T.rf_ptr[r + 1];
-      for (int f = f0; f < f1; ++f) {
-        float dv = M.keff32[r];
-        for (int g = f0; g < f1; ++g)
-          if (g != f) dv *= M.x32[T.rf_sp[g]];
-        M.d32[f] = dv;
+    const int32_t* rf_ptr = t<int32_t>(L.off_rf_ptr);
+    const int16_t* rf_sp = t<int16_t>(L.off_rf_sp);
+#pragma unroll 2
+    for (int r = lane; r < L.R; r += 32) {
+      const int f0 = rf_ptr[r], f1 = rf_ptr[r + 1];
+      const float kr = keff32[r];
+      if (f1 - f0 == 1) {
+        d32[f0] = kr;
+      } else if (f1 - f0 == 2) {
+        const float xa = x32[rf_sp[f0]], xb = x32[rf_sp[f0 + 1]];
+        d32[f0] = kr * xb;
+        d32[f0 + 1] = kr * xa;
+      } else {
+        for (int f = f0; f < f1; ++f) {
+          float dv = kr;
+          for (int g = f0; g < f1; ++g)
+            if (g != f) dv *= x32[rf_sp[g]];
+          d32[f] = dv;
+        }
       }
     }
     __syncwarp();
     const float c = static_cast<float>(coef);
-    for (int z = lane; z < NZ; z += 32) {
-      const int rc = T.jz_rc[z];
-      const int i = rc >> 16, j = rc & 0xffff;
-      float J = 0.f;
-      for (int e = T.jz_ptr[z]; e < T.jz_ptr[z + 1]; ++e) J += T.jc_nu32[e] * M.d32[T.jc_f[e]];
-      M.ustage[static_cast<size_t>(i) * LDU + j] = (i == j ? 1.f : 0.f) - c * J;
+    const int32_t* js_rc = t<int32_t>(L.off_js_rc);
+    const int32_t* js_cnt = t<int32_t>(L.off_js_cnt);
+    const int32_t* js_off = t<int32_t>(L.off_js_off);
+    const int16_t* jse_f = t<int16_t>(L.off_jse_f);
+    const float* jse_nu = t<float>(L.off_jse_nu32);
+    // Jacobian nonzeros over slices (sliced ELL): uniform trip counts, independent loads
+#pragma unroll 2
+    for (int sl = 0; sl < L.NJS; ++sl) {
+      const int rc = js_rc[sl * 32 + lane];
+      const int cnt = js_cnt[sl];
+      const int base = js_off[sl] + lane;
+      float J0 = 0.f, J1 = 0.f;
+      int cc = 0;
+      for (; cc + 2 <= cnt; cc += 2) {
+        const int e = base + 32 * cc;
+        const int f0 = jse_f[e], f1 = jse_f[e + 32];
+        J0 += jse_nu[e] * d32[f0];
+        J1 += jse_nu[e + 32] * d32[f1];
+      }
+      if (cc < cnt) J0 += jse_nu[base + 32 * cc] * d32[jse_f[base + 32 * cc]];
+      if (rc >= 0) {
+        const int i = rc >> 16, j = rc & 0xffff;
+        stage[i * LDU + j] = (i == j ? 1.f : 0.f) - c * (J0 + J1);
+      }
     }
     __syncwarp();
 #pragma unroll
     for (int s = 0; s < RPT; ++s) {
       const int i = row(s);
-      if (i < m) {
-        const float4* src = reinterpret_cast<const float4*>(M.ustage + static_cast<size_t>(i) * LDU);
+      if (i < mm) {
+        const float4* src = reinterpret_cast<const float4*>(stage + i * LDU);
 #pragma unroll
         for (int j4 = 0; j4 < MC / 4; ++j4) {
           const float4 v = src[j4];
@@ -185,58 +237,104 @@ struct Solver {
       }
     }
     __syncwarp();  // the staging area is overwritten by the U rows from here on
-    ++st.n_jac;
+    count(S_JAC);
+  }
+
+  // Rank-1 update with a one-column shift on groups [G0, G1): new A[j] = A[j+1] - l * U(k, k+1+j).
+  // All of the chunk's U loads are issued before its FMAs.
+  template <int G0, int G1>
+  __device__ __forceinline__ void update_chunk(const float (&l)[RPT], const float* urow) {
+    float4 u[G1 - G0];
+#pragma unroll
+    for (int g = G0; g < G1; ++g) u[g - G0] = reinterpret_cast<const float4*>(urow)[g];
+#pragma unroll
+    for (int g = G0; g < G1; ++g) {
+#pragma unroll
+      for (int s = 0; s < RPT; ++s) {
+        A[s][4 * g] = fmaf(-l[s], u[g - G0].x, A[s][4 * g + 1]);
+        A[s][4 * g + 1] = fmaf(-l[s], u[g - G0].y, A[s][4 * g + 2]);
+        A[s][4 * g + 2] = fmaf(-l[s], u[g - G0].z, A[s][4 * g + 3]);
+        A[s][4 * g + 3] = fmaf(-l[s], u[g - G0].w, (4 * g + 4 < MC) ? A[s][4 * g + 4] : 0.f);
+      }
+    }
+  }
+
+  // Pivot key of this lane's active rows: |a| bits with the low 6 mantissa bits replaced by
+  // 63 - row, so one redux.sync.max picks the row of largest magnitude (up to a relative 2^-17),
+  // ties to the lowest row.
+  __device__ __forceinline__ uint32_t pivot_key(const bool (&act)[RPT]) const {
+    uint32_t key = 0u;
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) {
+      const uint32_t kb = ((__float_as_uint(A[s][0]) & 0x7fffffffu) & ~63u) | static_cast<uint32_t>(63 - row(s));
+      key = max(key, act[s] ? kb : 0u);
+    }
+    return key;
   }
 
   // ---- LU with the forward substitution of wf fused in --------------------------------------
   // wf: in, the FP32 right-hand side by row; out, the forward-eliminated values by row. On return
-  // M.ybuf holds the same values in step order. Returns false on a zero or non-finite pivot.
+  // ybuf holds the same values in step order. Returns false on a zero or non-finite pivot.
+  //
+  // The pivot row's U part is published with predicated (branch-free) stores by its owner lane;
+  // the next step's pivot reduction is issued as soon as the first column group is updated, so
+  // its latency overlaps the rest of the update.
   __device__ __forceinline__ bool factor_fwd(float (&wf)[RPT]) {
+    static_assert(32 * RPT <= 64, "row index must fit the 6 key bits");
+    constexpr int NG = MC / 4;
+    constexpr int C1 = (NG + 2) / 3, C2 = (2 * NG + 2) / 3;
+    const int mm = m();
+    float* ustage = w<float>(P.ml.ustage);
+    float* lrow = w<float>(P.ml.lrow);
+    float* pinv_s = w<float>(P.ml.pinv);
+    float* ybuf = w<float>(P.ml.ybuf);
+    int* piv = w<int>(P.ml.piv);
+    const int LDL = P.ml.LDL;
     bool act[RPT];
 #pragma unroll
     for (int s = 0; s < RPT; ++s) {
-      act[s] = row(s) < m;
+      act[s] = row(s) < mm;
       step[s] = INT_MAX;
     }
+    uint32_t gk = __reduce_max_sync(kFullMask, pivot_key(act));
 #pragma unroll 1
-    for (int k = 0; k < m; ++k) {
-      uint32_t vb[RPT];
-      uint32_t lm = 0u;
-#pragma unroll
-      for (int s = 0; s < RPT; ++s) {
-        vb[s] = act[s] ? (__float_as_uint(A[s][0]) & 0x7fffffffu) : 0u;
-        lm = max(lm, vb[s]);
-      }
-      const uint32_t gm = __reduce_max_sync(kFullMask, lm);
-      if (gm == 0u || gm >= 0x7f800000u) return false;  // zero column, inf or nan
-      int p = -1;
-#pragma unroll
-      for (int s = 0; s < RPT; ++s) {
-        const unsigned bal = __ballot_sync(kFullMask, vb[s] == gm);
-        if (p < 0 && bal != 0u) p = (__ffs(bal) - 1) + 32 * s;
-      }
+    for (int k = 0; k < mm; ++k) {
+      if ((gk >> 6) == 0u || (gk & ~63u) >= 0x7f800000u) return false;  // zero column, inf or nan
+      const int p = 63 - static_cast<int>(gk & 63u);
       const int owner = p & 31, pslot = p >> 5;
-      const int width = m - 1 - k;  // trailing columns after the pivot
-      float* urow = M.ustage + static_cast<size_t>(k) * LDU;
-      if (lane == owner) {
+      const bool is_owner = lane == owner;
+      float pv_mine = A[0][0], w_mine = wf[0];
 #pragma unroll
-        for (int s = 0; s < RPT; ++s) {
-          if (s == pslot) {
+      for (int s = 1; s < RPT; ++s)
+        if (pslot == s) { pv_mine = A[s][0]; w_mine = wf[s]; }
+      // publish the pivot row's U part (registers 1..MC-1) with predicated stores
+      float* urow = ustage + k * LDU;
+      const uint32_t ua = static_cast<uint32_t>(__cvta_generic_to_shared(urow));
 #pragma unroll
-            for (int g = 0; g < MC / 4; ++g) {
-              if (4 * g < width)
-                reinterpret_cast<float4*>(urow)[g] =
-                    make_float4(A[s][4 * g + 1], A[s][4 * g + 2], A[s][4 * g + 3], (4 * g + 4 < MC) ? A[s][4 * g + 4] : 0.f);
-            }
-            M.pinv[k] = __frcp_rn(A[s][0]);
-            M.ybuf[k] = wf[s];
-            M.piv[k] = p;
-          }
+      for (int g = 0; g < NG; ++g) {
+        float v[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int j = 4 * g + q + 1;
+          v[q] = j < MC ? A[0][j] : 0.f;
+#pragma unroll
+          for (int s = 1; s < RPT; ++s)
+            if (pslot == s) v[q] = j < MC ? A[s][j] : 0.f;
         }
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %0, 0;\n @p st.shared.v4.f32 [%1], {%2, %3, %4, %5};\n}\n" ::"r"(
+                static_cast<int>(is_owner)),
+            "r"(ua + 16u * g), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
+            : "memory");
       }
-      __syncwarp();
-      const float pinv = M.pinv[k];
-      const float yk = M.ybuf[k];
+      const float pval = __shfl_sync(kFullMask, pv_mine, owner);
+      const float yk = __shfl_sync(kFullMask, w_mine, owner);
+      const float pinv = __fdividef(1.f, pval);
+      if (is_owner) {
+        pinv_s[k] = pinv;
+        ybuf[k] = yk;
+        piv[k] = p;
+      }
       float l[RPT];
 #pragma unroll
       for (int s = 0; s < RPT; ++s) {
@@ -246,35 +344,38 @@ struct Solver {
         }
         l[s] = act[s] ? A[s][0] * pinv : 0.f;
         if (act[s]) {
-          M.lrow[static_cast<size_t>(row(s)) * LDL + k] = l[s];
+          lrow[row(s) * LDL + k] = l[s];
           wf[s] = fmaf(-l[s], yk, wf[s]);
         }
       }
-      // rank-1 update with a one-column shift: new A[j] = A[j+1] - l * U(k, k+1+j)
-#pragma unroll
-      for (int g = 0; g < MC / 4; ++g) {
-        if (4 * g < width) {
-          const float4 u = reinterpret_cast<const float4*>(urow)[g];
-#pragma unroll
-          for (int s = 0; s < RPT; ++s) {
-            A[s][4 * g] = fmaf(-l[s], u.x, A[s][4 * g + 1]);
-            A[s][4 * g + 1] = fmaf(-l[s], u.y, A[s][4 * g + 2]);
-            A[s][4 * g + 2] = fmaf(-l[s], u.z, A[s][4 * g + 3]);
-            A[s][4 * g + 3] = fmaf(-l[s], u.w, (4 * g + 4 < MC) ? A[s][4 * g + 4] : 0.f);
-          }
-        }
+      __syncwarp();
+      // first group (holds the next pivot column), then the next step's pivot reduction, then
+      // the rest of the update
+      update_chunk<0, 1>(l, urow);
+      gk = __reduce_max_sync(kFullMask, pivot_key(act));
+      const int width = mm - 1 - k;
+      update_chunk<1, C1>(l, urow);
+      if (4 * C1 < width) {
+        update_chunk<C1, C2>(l, urow);
+        if (4 * C2 < width) update_chunk<C2, NG>(l, urow);
       }
+      __syncwarp();
     }
-    __syncwarp();
-    ++st.n_lu;
+    count(S_LU);
     return true;
   }
 
-  // Forward substitution with the stored multipliers (rows' values in wf, in place).
+  // Forward substitution with the stored multipliers (rows' values in wf, in place); leaves the
+  // values in step order in ybuf.
   __device__ __forceinline__ void forward(float (&wf)[RPT]) {
+    const int mm = m();
+    const float* lrow = w<float>(P.ml.lrow);
+    const int* piv = w<int>(P.ml.piv);
+    float* ybuf = w<float>(P.ml.ybuf);
+    const int LDL = P.ml.LDL;
 #pragma unroll 1
-    for (int k = 0; k < m; ++k) {
-      const int p = M.piv[k];
+    for (int k = 0; k < mm; ++k) {
+      const int p = piv[k];
       float mine = 0.f;
 #pragma unroll
       for (int s = 0; s < RPT; ++s)
@@ -282,27 +383,30 @@ struct Solver {
       const float yk = __shfl_sync(kFullMask, mine, p & 31);
 #pragma unroll
       for (int s = 0; s < RPT; ++s)
-        if (step[s] > k && row(s) < m) wf[s] = fmaf(-M.lrow[static_cast<size_t>(row(s)) * LDL + k], yk, wf[s]);
+        if (step[s] > k && row(s) < mm) wf[s] = fmaf(-lrow[row(s) * LDL + k], yk, wf[s]);
     }
-    // values by step for the back substitution
 #pragma unroll
     for (int s = 0; s < RPT; ++s)
-      if (row(s) < m) M.ybuf[step[s]] = wf[s];
+      if (row(s) < mm) ybuf[step[s]] = wf[s];
     __syncwarp();
   }
 
-  // Back substitution from M.ybuf (values in step order) to x in species order.
+  // Back substitution from ybuf (values in step order) to x in species order.
   __device__ __forceinline__ void backward(double (&x)[RPT]) {
+    const int mm = m();
+    const float* ustage = w<float>(P.ml.ustage);
+    const float* ybuf = w<float>(P.ml.ybuf);
+    const float* pinv_s = w<float>(P.ml.pinv);
     float ys[RPT], pv[RPT], xs[RPT];
 #pragma unroll
     for (int s = 0; s < RPT; ++s) {
-      ys[s] = row(s) < m ? M.ybuf[row(s)] : 0.f;
-      pv[s] = row(s) < m ? M.pinv[row(s)] : 0.f;
+      ys[s] = row(s) < mm ? ybuf[row(s)] : 0.f;
+      pv[s] = row(s) < mm ? pinv_s[row(s)] : 0.f;
       xs[s] = 0.f;
     }
     __syncwarp();
 #pragma unroll 1
-    for (int k = m - 1; k >= 0; --k) {
+    for (int k = mm - 1; k >= 0; --k) {
       float mine = 0.f;
 #pragma unroll
       for (int s = 0; s < RPT; ++s)
@@ -311,22 +415,13 @@ struct Solver {
 #pragma unroll
       for (int s = 0; s < RPT; ++s) {
         const int i = row(s);
-        if (i < k) ys[s] = fmaf(-M.ustage[static_cast<size_t>(i) * LDU + (k - i - 1)], xk, ys[s]);
+        if (i < k) ys[s] = fmaf(-ustage[i * (LDU - 1) + k - 1], xk, ys[s]);
         if (i == k) xs[s] = xk;
       }
     }
 #pragma unroll
     for (int s = 0; s < RPT; ++s) x[s] = static_cast<double>(xs[s]);
-    ++st.n_solve;
-  }
-
-  // x = A^{-1} b with the stored factors.
-  __device__ __forceinline__ void solve(const double (&b)[RPT], double (&x)[RPT]) {
-    float wf[RPT];
-#pragma unroll
-    for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(b[s]);
-    forward(wf);
-    backward(x);
+    count(S_SOLVE);
   }
 
   // ---- Newton on y - coef f(y) = rhs --------------------------------------------------------
@@ -345,11 +440,11 @@ struct Solver {
         forward(wf);
       }
       backward(dx);
-      ++st.n_newton_iter;
+      count(S_NEWTON);
       double sdx = 0.0, sy = 0.0;
 #pragma unroll
       for (int s = 0; s < RPT; ++s) {
-        if (row(s) < m) {
+        if (row(s) < m()) {
           y[s] += dx[s];
           sdx += dx[s] * dx[s];
           sy += y[s] * y[s];
@@ -362,11 +457,17 @@ struct Solver {
     return false;
   }
 
+  // Stores a row-distributed vector into the shared stage-vector slot v.
+  __device__ __forceinline__ void put(int v, const double (&a)[RPT]) const {
+#pragma unroll
+    for (int s = 0; s < RPT; ++s)
+      if (row(s) < m()) vec(v, row(s)) = a[s];
+  }
+
   // ---- TR-BDF2 (the algorithm of the plain kernel and of the oracle) ------------------------
-  __device__ __forceinline__ int integrate(double (&y)[RPT], const double (&atol)[RPT], const double (&rtol)[RPT],
-                                           double t_beg, double t_end, double dt_in, double dt_min, double dt_max,
-                                           int max_iters, int max_newton, int jac_interval, double natol,
-                                           double nrtol, double& t_out, double& dt_out) {
+  __device__ __forceinline__ int integrate(double (&y)[RPT], double t_beg, double t_end, double dt_in, double dt_min,
+                                           double dt_max, int max_iters, int max_newton, int jac_interval,
+                                           double natol, double nrtol, double& t_out, double& dt_out) {
     if (dt_in < 0.0) return TCHEM_GB_SAMPLE_NEGATIVE_DT;
     const double gamma = 2.0 - sqrt(2.0);
     const double d = 0.5 * gamma;
@@ -374,10 +475,14 @@ struct Solver {
     const double cn = (1.0 - gamma) * (1.0 - gamma) / (gamma * (2.0 - gamma));
     const double kappa = (-3.0 * gamma * gamma + 4.0 * gamma - 2.0) / (12.0 * (2.0 - gamma));
     const double e0 = 1.0 / gamma, e1 = -1.0 / (gamma * (1.0 - gamma)), e2 = 1.0 / (1.0 - gamma);
-    double fn[RPT], fg[RPT], f1[RPT], yg[RPT], y1[RPT], rv[RPT];
+    double yg[RPT], y1[RPT];
     double t = t_beg, dt = dt_in;
     int status = TCHEM_GB_SAMPLE_OK;
-    rhs(y, fn);
+    {
+      double fn[RPT];
+      rhs(y, fn);
+      put(V_FN, fn);
+    }
     for (int iter = 0; iter < max_iters && t < t_end; ++iter) {
       bool converged = false, last = false;
       for (int ntry = 0; ntry < 4; ++ntry) {
@@ -390,10 +495,11 @@ struct Solver {
         bool ok = true;
 #pragma unroll 1
         for (int stage = 0; stage < 2 && ok; ++stage) {
-          double guess[RPT];
+          double guess[RPT], rv[RPT];
 #pragma unroll
           for (int s = 0; s < RPT; ++s) {
-            rv[s] = stage == 0 ? y[s] + coef * fn[s] : cg * yg[s] - cn * y[s];
+            const int i = row(s) < m() ? row(s) : 0;
+            rv[s] = stage == 0 ? y[s] + coef * vec(V_FN, i) : cg * yg[s] - cn * y[s];
             guess[s] = stage == 0 ? y[s] : yg[s];
           }
           ok = newton(guess, rv, coef, max_newton, jac_interval, natol, nrtol);
@@ -403,25 +509,39 @@ struct Solver {
               if (stage == 0) yg[s] = guess[s];
               else y1[s] = guess[s];
             }
-            if (stage == 0) rhs(yg, fg);
+            if (stage == 0) {
+              double fg[RPT];
+              rhs(yg, fg);
+              put(V_FG, fg);
+            }
           }
         }
         if (ok) { converged = true; break; }
-        ++st.n_newton_fail;
+        count(S_NFAIL);
         dt *= 0.5;
       }
       if (status != TCHEM_GB_SAMPLE_OK) break;
       if (!converged) { status = TCHEM_GB_SAMPLE_NEWTON_FAIL; break; }
+      double f1[RPT], estf[RPT];
       rhs(y1, f1);
-      double est[RPT], estf[RPT];
+      {
+        double est[RPT];
 #pragma unroll
-      for (int s = 0; s < RPT; ++s) est[s] = 2.0 * kappa * dt * (e0 * fn[s] + e1 * fg[s] + e2 * f1[s]);
-      solve(est, estf);
+        for (int s = 0; s < RPT; ++s) {
+          const int i = row(s) < m() ? row(s) : 0;
+          est[s] = 2.0 * kappa * dt * (e0 * vec(V_FN, i) + e1 * vec(V_FG, i) + e2 * f1[s]);
+        }
+        float wf[RPT];
+#pragma unroll
+        for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(est[s]);
+        forward(wf);
+        backward(estf);
+      }
       double err = 0.0;
 #pragma unroll
       for (int s = 0; s < RPT; ++s) {
-        if (row(s) < m) {
-          const double wgt = atol[s] + rtol[s] * fmax(fabs(y[s]), fabs(y1[s]));
+        if (row(s) < m()) {
+          const double wgt = vec(V_ATOL, row(s)) + vec(V_RTOL, row(s)) * fmax(fabs(y[s]), fabs(y1[s]));
           err = fmax(err, fabs(estf[s]) / wgt);
         }
       }
@@ -430,16 +550,18 @@ struct Solver {
       if (err <= 1.0 || dt <= dt_min) {
         t = last ? t_end : t + dt;
 #pragma unroll
-        for (int s = 0; s < RPT; ++s) { y[s] = y1[s]; fn[s] = f1[s]; }
-        ++st.n_steps;
+        for (int s = 0; s < RPT; ++s) y[s] = y1[s];
+        put(V_FN, f1);
+        count(S_STEPS);
         double fac = err > 0.0 ? 0.9 * cbrt(1.0 / err) : 2.0;
         fac = fmax(0.2, fmin(2.0, fac));
         dt = fmin(dt * fac, dt_max);
         if (t + dt > t_end) dt = t_end - t;
       } else {
-        ++st.n_rejected;
+        count(S_REJ);
         dt *= fmax(0.2, 0.9 * cbrt(1.0 / err));
       }
+      __syncwarp();
     }
     t_out = t;
     dt_out = dt;
@@ -465,22 +587,19 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
     return;
   }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const size_t gbytes = group_smem_bytes(L, MC);
-  Solver<MC, RPT> S;
-  S.T = tables_at(tables, L);
-  S.M = carve(tables + L.blob_bytes + warp * gbytes, L, MC);
-  S.m = L.m;
-  S.R = L.R;
-  S.NZ = L.NZ;
-  S.lane = lane;
-  S.LDL = ldl_for(L.m);
+  Solver<MC, RPT> S{P, tables, tables + L.blob_bytes + warp * P.ml.warp_bytes, lane};
   const int m = L.m;
   const int n_items = P.n_items_dev ? *P.n_items_dev : P.n_items;
+  int* stats = S.template w<int>(P.ml.stats);
+  double* keff = S.template w<double>(P.ml.keff);
+  float* keff32 = S.template w<float>(P.ml.keff32);
+  int* item_s = S.template w<int>(P.ml.item);
 
   while (true) {
-    int item = 0;
-    if (lane == 0) item = atomicAdd(P.queue, 1);
-    item = __shfl_sync(kFullMask, item, 0);
+    if (lane == 0) item_s[0] = atomicAdd(P.queue, 1);
+    __syncwarp();
+    const int item = item_s[0];
+    __syncwarp();
     if (item >= n_items) break;
     const int smp = P.items ? P.items[item] : item;
     const tchem_gb_tadv ta = P.tadv[smp];
@@ -506,28 +625,45 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
       for (int r = lane; r < L.R; r += 32) {
         double k = rate_constant(P.mech.rate_type[r], rp + 8 * r, P.mech.conv_exp[r], Tk, t_1, p, conv);
         for (int c = P.mech.cf_ptr[r]; c < P.mech.cf_ptr[r + 1]; ++c) k *= row[3 + m + P.mech.cf_idx[c]];
-        S.M.keff[r] = k;
-        S.M.keff32[r] = static_cast<float>(k);
+        keff[r] = k;
+        keff32[r] = static_cast<float>(k);
       }
     }
+    for (int i = lane; i < m; i += 32) {
+      S.vec(V_ATOL, i) = P.tol_time[2 * i];
+      S.vec(V_RTOL, i) = P.tol_time[2 * i + 1];
+    }
+    if (lane < 8) stats[lane] = 0;
+    if (lane == 0) {
+      S.template w<double>(P.ml.q)[L.R] = 0.0;
+      S.template w<float>(P.ml.d32)[L.NF] = 0.f;
+    }
     __syncwarp();
-    S.st = tchem_gb_sample_stats{};
-    double y[RPT], atol[RPT], rtol[RPT];
+    double y[RPT];
 #pragma unroll
     for (int s = 0; s < RPT; ++s) {
       const int i = S.row(s);
       y[s] = (i < m) ? row[3 + i] : 0.0;
-      atol[s] = (i < m) ? P.tol_time[2 * i] : 1.0;
-      rtol[s] = (i < m) ? P.tol_time[2 * i + 1] : 0.0;
     }
     double t_o = 0.0, dt_o = 0.0;
     const int jac_int = ta.jacobian_interval > 0 ? ta.jacobian_interval : 1;
-    const int stt = S.integrate(y, atol, rtol, ta.tbeg, ta.tend, ta.dt, ta.dtmin, ta.dtmax,
-                                ta.num_time_iterations_per_interval, ta.max_num_newton_iterations, jac_int,
-                                P.tol_newton[0], P.tol_newton[1], t_o, dt_o);
+    const int stt = S.integrate(y, ta.tbeg, ta.tend, ta.dt, ta.dtmin, ta.dtmax, ta.num_time_iterations_per_interval,
+                                ta.max_num_newton_iterations, jac_int, P.tol_newton[0], P.tol_newton[1], t_o, dt_o);
+    __syncwarp();
     if (lane == 0) {
       P.status[smp] = stt;
-      if (P.stats) P.stats[smp] = S.st;
+      if (P.stats) {
+        tchem_gb_sample_stats sst;
+        sst.n_steps = stats[S_STEPS];
+        sst.n_rejected = stats[S_REJ];
+        sst.n_newton_fail = stats[S_NFAIL];
+        sst.n_newton_iter = stats[S_NEWTON];
+        sst.n_lu = stats[S_LU];
+        sst.n_solve = stats[S_SOLVE];
+        sst.n_rhs = stats[S_RHS];
+        sst.n_jac = stats[S_JAC];
+        P.stats[smp] = sst;
+      }
     }
     if (stt != TCHEM_GB_SAMPLE_NEGATIVE_DT) {
       double* out = P.state_out + static_cast<size_t>(smp) * P.state_dim;
