@@ -26,7 +26,7 @@ def load() -> C.CDLL:
         L.oracle_jacobian.argtypes = [vp, C.c_double, C.c_double, vp, vp]
         L.oracle_time_advance.restype = C.c_int
         L.oracle_time_advance.argtypes = [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp,
-                                          C.c_int, C.c_int]
+                                          C.c_int, C.c_int, C.c_int]
         _lib = L
     return _lib
 
@@ -71,10 +71,11 @@ class Oracle:
 
     def time_advance(self, tadv: np.ndarray, state: np.ndarray, tol_newton, tol_time: np.ndarray,
                      t_out: np.ndarray | None = None, mech_of_sample: np.ndarray | None = None,
-                     lu_fp32: int = 0, nthreads: int = 0):
+                     lu_fp32: int = 0, nthreads: int = 0, simplified: bool = False):
         """Returns (state_out, t_out, dt_out, status, stats).
 
         lu_fp32: 0 FP64 LU; k >= 1 FP32 LU with k - 1 refinement sweeps after Newton convergence.
+        simplified: the simplified-Newton form (factors carried across iterations and steps).
         """
         B = state.shape[0]
         state = np.ascontiguousarray(state, dtype=np.float64)
@@ -90,7 +91,7 @@ class Oracle:
         tadv = np.ascontiguousarray(tadv)
         rc = self.lib.oracle_time_advance(self._ptrs, len(self._views), _p(mos), B, _p(tn), _p(tt), _p(tadv),
                                           _p(state), _p(t_out), _p(dt_out), _p(state_out), _p(status), _p(stats),
-                                          int(lu_fp32), int(nthreads))
+                                          int(lu_fp32), int(bool(simplified)), int(nthreads))
         if rc != 0:
             raise RuntimeError(f"oracle_time_advance returned {rc}")
         return state_out, t_out, dt_out, status, stats

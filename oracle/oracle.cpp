@@ -5,6 +5,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <limits>
 #include <vector>
 
 #ifdef _OPENMP
@@ -171,6 +172,7 @@ struct DenseLU {
 
 struct Settings {
   int max_newton, jac_interval, max_iters, refine;
+  bool simplified;  // simplified-Newton form (tchem_gb.h, TCHEM_GB_FORM_MIXED_SIMPLIFIED)
   double atol_newton, rtol_newton;
   const double* tol_time;  // [m][2]
 };
@@ -183,6 +185,9 @@ struct Sample {
   std::vector<double> kfor, rop, concX, J;
   DenseLU<LU_T> lu;
   tchem_gb_sample_stats st{};
+  // simplified-Newton form: factors valid / formed in the current stage, and their coefficient
+  bool have_lu = false, fresh = false;
+  double c_lu = 0.0;
 
   Sample(const tchem_gb_kmcd_view& km_, double T, double p, const double* xconst)
       : km(km_), m(km_.nSpec - km_.nConstSpec), n(km_.nSpec) {
@@ -205,9 +210,53 @@ struct Sample {
     ++st.n_jac;
   }
 
+  // Simplified Newton: the factors of I - c_lu J (carried, or formed at the first iterate) serve
+  // every iteration; they are re-formed once per stage at the current iterate when the max-norm
+  // of the correction (rounded to FP32) shrinks by less than half. Converged when every
+  // |dx_i| <= atol / sqrt(m) + rtol |y_i|, which implies the 2-norm test of the full Newton
+  // method (||dx|| <= atol + rtol ||y||, by Minkowski's inequality).
+  bool newton_simplified(double* y, const double* rhs, double c, const Settings& s, std::vector<double>& fy,
+                         std::vector<double>& g, std::vector<double>& dx) {
+    float prev = 0.f;
+    bool refresh = !have_lu;
+    const double atol_c = s.atol_newton / std::sqrt(static_cast<double>(m));
+    for (int it = 0; it < s.max_newton; ++it) {
+      f(y, fy.data());
+      for (int i = 0; i < m; ++i) g[i] = -((y[i] - c * fy[i]) - rhs[i]);
+      if (refresh) {
+        jac(y);
+        if (!lu.factor(J.data(), c)) return false;
+        ++st.n_lu;
+        have_lu = fresh = true;
+        refresh = false;
+        c_lu = c;
+      }
+      lu.solve(g.data(), dx.data());
+      ++st.n_solve;
+      ++st.n_newton_iter;
+      bool finite = true, conv = true;
+      float dmax = 0.f;
+      for (int i = 0; i < m; ++i) {
+        y[i] += dx[i];
+        finite = finite && std::isfinite(dx[i]) && std::isfinite(y[i]);
+        conv = conv && std::abs(dx[i]) <= atol_c + s.rtol_newton * std::abs(y[i]);
+        dmax = std::max(dmax, static_cast<float>(std::abs(dx[i])));
+      }
+      if (!finite) return false;
+      if (it > 0 && !fresh && dmax > 0.5f * prev) refresh = true;
+      prev = dmax;
+      if (conv) return true;
+    }
+    return false;
+  }
+
   // Solves y - c f(y) = rhs by Newton from the guess in y.
   bool newton(double* y, const double* rhs, double c, const Settings& s, std::vector<double>& fy,
               std::vector<double>& g, std::vector<double>& dx) {
+    if (s.simplified) {
+      fresh = false;
+      return newton_simplified(y, rhs, c, s, fy, g, dx);
+    }
     for (int it = 0; it < s.max_newton; ++it) {
       f(y, fy.data());
       for (int i = 0; i < m; ++i) g[i] = -((y[i] - c * fy[i]) - rhs[i]);
@@ -255,6 +304,9 @@ struct Sample {
     std::vector<double> fn(m), fg(m), f1(m), yg(m), y1(m), rhs(m), fy(m), g(m), dx(m), est(m), estf(m);
     double t = t_beg, dt = dt_in;
     int status = TCHEM_GB_SAMPLE_OK;
+    std::vector<double> yp(m), ygp(m);  // simplified form: last accepted step's y_n and y_gamma
+    double dtp = 0.0;
+    bool have_prev = false;
     f(y, fn.data());
     for (int iter = 0; iter < s.max_iters && t < t_end; ++iter) {
       bool converged = false, last = false;
@@ -264,13 +316,28 @@ struct Sample {
         if (last) dt = t_end - t;
         if (!(dt > 0.0)) { status = TCHEM_GB_SAMPLE_DT_UNDERFLOW; break; }
         const double c = d * dt;
+        // simplified form: keep the carried factors while c moved by at most 30%
+        if (s.simplified && !(have_lu && std::abs(c / c_lu - 1.0) <= 0.3)) have_lu = false;
         // stage 1 (trapezoidal rule to t + gamma dt)
         for (int i = 0; i < m; ++i) { rhs[i] = y[i] + c * fn[i]; yg[i] = y[i]; }
+        if (s.simplified && have_prev) {
+          // stage-1 guess: the quadratic through the last step's y_{n-1}, y_{n-1+gamma}, y_n
+          const double t0 = -dtp, t1 = -(1.0 - gamma) * dtp, tt = gamma * dt;
+          const double l0 = (tt - t1) * tt / ((t0 - t1) * t0);
+          const double l1 = (tt - t0) * tt / ((t1 - t0) * t1);
+          const double l2 = (tt - t0) * (tt - t1) / (t0 * t1);
+          for (int i = 0; i < m; ++i) yg[i] = l0 * yp[i] + l1 * ygp[i] + l2 * y[i];
+        }
         bool ok = newton(yg.data(), rhs.data(), c, s, fy, g, dx);
         if (ok) {
           // stage 2 (BDF2 through t, t + gamma dt, t + dt)
           f(yg.data(), fg.data());
           for (int i = 0; i < m; ++i) { rhs[i] = cg * yg[i] - cn * y[i]; y1[i] = yg[i]; }
+          if (s.simplified) {
+            // stage-2 guess: the quadratic with p(t) = y_n, p'(t) = f_n, p(t + gamma dt) = y_gamma
+            const double a = 1.0 / (gamma * gamma), b = dt * (1.0 - 1.0 / gamma);
+            for (int i = 0; i < m; ++i) y1[i] = (1.0 - a) * y[i] + a * yg[i] + b * fn[i];
+          }
           ok = newton(y1.data(), rhs.data(), c, s, fy, g, dx);
         }
         if (ok) { converged = true; break; }
@@ -282,8 +349,22 @@ struct Sample {
       f(y1.data(), f1.data());
       // local error estimate, filtered through (I - d dt J)^{-1}
       for (int i = 0; i < m; ++i) est[i] = 2.0 * kappa * dt * (e0 * fn[i] + e1 * fg[i] + e2 * f1[i]);
-      lu.solve(est.data(), estf.data());
-      ++st.n_solve;
+      if (s.simplified) {
+        // filter with the factors of I - c J(y_{n+1}), carried into the next step
+        jac(y1.data());
+        have_lu = lu.factor(J.data(), d * dt);
+        c_lu = d * dt;
+        if (have_lu) {
+          ++st.n_lu;
+          lu.solve(est.data(), estf.data());
+          ++st.n_solve;
+        } else {
+          std::fill(estf.begin(), estf.end(), std::numeric_limits<double>::quiet_NaN());
+        }
+      } else {
+        lu.solve(est.data(), estf.data());
+        ++st.n_solve;
+      }
       double err = 0.0;
       for (int i = 0; i < m; ++i) {
         const double w = s.tol_time[2 * i] + s.tol_time[2 * i + 1] * std::max(std::abs(y[i]), std::abs(y1[i]));
@@ -292,6 +373,12 @@ struct Sample {
       if (!std::isfinite(err)) { status = TCHEM_GB_SAMPLE_NONFINITE; break; }
       if (err <= 1.0 || dt <= dt_min) {
         t = last ? t_end : t + dt;
+        if (s.simplified) {
+          std::copy(y, y + m, yp.begin());
+          ygp = yg;
+          dtp = dt;
+          have_prev = true;
+        }
         std::copy(y1.begin(), y1.end(), y);
         fn.swap(f1);
         ++st.n_steps;
@@ -318,7 +405,8 @@ struct Sample {
 template <typename LU_T>
 void run_batch(const tchem_gb_kmcd_view* const* kms, const int32_t* mech_of_sample, int nbatch, const double* tol_newton,
                const double* tol_time, const tchem_gb_tadv* tadv, const double* state, double* t_out,
-               double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats, int dim, int refine) {
+               double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats, int dim, int refine,
+               bool simplified) {
 #pragma omp parallel for schedule(dynamic, 1)
   for (int b = 0; b < nbatch; ++b) {
     const tchem_gb_kmcd_view& km = *kms[mech_of_sample ? mech_of_sample[b] : 0];
@@ -337,7 +425,7 @@ void run_batch(const tchem_gb_kmcd_view* const* kms, const int32_t* mech_of_samp
     std::vector<double> xconst(row + 3 + m, row + 3 + n);
     Sample<LU_T> smp(km, T, p, xconst.data());
     Settings s{ta.max_num_newton_iterations, std::max(1, ta.jacobian_interval), ta.num_time_iterations_per_interval,
-               refine, tol_newton[0], tol_newton[1], tol_time};
+               refine, simplified, tol_newton[0], tol_newton[1], tol_time};
     double to = 0.0, dto = 0.0;
     const int st = smp.integrate(y.data(), ta.tbeg, ta.tend, ta.dt, ta.dtmin, ta.dtmax, s, to, dto);
     if (status) status[b] = st;
@@ -382,7 +470,7 @@ int oracle_jacobian(const tchem_gb_kmcd_view* km, double T, double p, const doub
 int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const int32_t* mech_of_sample, int nbatch,
                         const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
                         const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
-                        tchem_gb_sample_stats* stats, int lu_fp32, int nthreads) {
+                        tchem_gb_sample_stats* stats, int lu_fp32, int simplified, int nthreads) {
   if (!kms || n_mechs <= 0 || nbatch < 0 || !tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out ||
       !state_out)
     return TCHEM_GB_ERR_ARG;
@@ -398,10 +486,10 @@ int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const
 #endif
   if (lu_fp32)
     run_batch<float>(kms, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status,
-                     stats, dim, lu_fp32 - 1);
+                     stats, dim, lu_fp32 - 1, simplified != 0);
   else
     run_batch<double>(kms, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status,
-                      stats, dim, 0);
+                      stats, dim, 0, simplified != 0);
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(prev);
 #endif

@@ -45,12 +45,16 @@ int oracle_jacobian(const tchem_gb_kmcd_view* km, double T, double p, const doub
  * lu_fp32 = 0: FP64 Newton LU (the plain form); k >= 1: FP32 LU and solves with FP64 residuals
  * and k - 1 refinement sweeps after Newton convergence (the algorithm of the engine's
  * mixed-precision form, for like-for-like checks).
+ * simplified != 0: the simplified-Newton form of TCHEM_GB_FORM_MIXED_SIMPLIFIED (factors carried
+ * across Newton iterations and steps, componentwise Newton test, error filter with I - c J(y_{n+1}));
+ * the factors are LU here and a Gauss-Jordan inverse in the engine, which agree to the Newton
+ * tolerance.
  * t_out is read (samples with t_out >= tend are skipped) and written.
  * nthreads <= 0 uses all OpenMP threads. stats may be NULL. */
 int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const int32_t* mech_of_sample, int nbatch,
                         const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
                         const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
-                        tchem_gb_sample_stats* stats, int lu_fp32, int nthreads);
+                        tchem_gb_sample_stats* stats, int lu_fp32, int simplified, int nthreads);
 
 #ifdef __cplusplus
 }

@@ -112,12 +112,14 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
   }
   const DeviceInfo info = device_info(dev);
   for (auto& g : plan.groups) {
-    if (o.form == TCHEM_GB_FORM_MIXED) g.dev = dts[g.mechs[0]]->dev_x;  // sliced-ELL tables
+    const bool mixed = o.form == TCHEM_GB_FORM_MIXED || o.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED;
+    if (mixed) g.dev = dts[g.mechs[0]]->dev_x;  // sliced-ELL tables
     const MechLayout& L = g.dev.L;
     plan.m_max = std::max(plan.m_max, L.m);
     g.form = o.form;
-    if (o.form == TCHEM_GB_FORM_MIXED) {
-      MixedConfig mc = mixed_config(L, o.threads_per_sample, info.sm_count, info.max_smem_optin, nbatch);
+    if (mixed) {
+      MixedConfig mc = mixed_config(L, o.threads_per_sample, info.sm_count, info.max_smem_optin, nbatch,
+                                    o.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED);
       g.kernel = mc.kernel;
       g.warps_per_block = mc.warps_per_block;
       g.grid = mc.grid;
@@ -248,7 +250,7 @@ int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const 
   if (!tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out || !state_out || !status)
     return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance: null argument");
   const tchem_gb_advance_opts o = opts_or_default(opts);
-  if (o.form != TCHEM_GB_FORM_PLAIN_FP64 && o.form != TCHEM_GB_FORM_MIXED)
+  if (o.form != TCHEM_GB_FORM_PLAIN_FP64 && o.form != TCHEM_GB_FORM_MIXED && o.form != TCHEM_GB_FORM_MIXED_SIMPLIFIED)
     return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance: unknown form");
   cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
   int dev = 0;
@@ -326,7 +328,7 @@ int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const 
     P.warp_smem_bytes = gp.warp_smem;
     P.error_word = error_word;
     P.ml = gp.ml;
-    if (gp.form == TCHEM_GB_FORM_MIXED)
+    if (gp.form == TCHEM_GB_FORM_MIXED || gp.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED)
       e = launch_trbdf2_mixed(P, gp.dev.L, gp.grid, gp.warps_per_block, gp.smem, gp.threads_per_sample, stream);
     else
       e = launch_trbdf2_fp64(P, gp.grid, gp.warps_per_block, gp.smem, stream);

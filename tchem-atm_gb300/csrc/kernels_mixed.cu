@@ -53,12 +53,13 @@ const Variant* pick(const MechLayout& L) {
 
 }  // namespace
 
-MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch) {
+MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch,
+                         bool simplified) {
   if (threads_per_sample != 0 && threads_per_sample != 32)
     throw std::domain_error("mixed form: threads_per_sample must be 0 or 32");
   const Variant* best = pick(L);
   if (!best) throw std::domain_error("mixed form: mechanisms with more than 64 active species are not supported");
-  const MixedLayout ml = mixed::make_layout(L, best->MC);
+  const MixedLayout ml = mixed::make_layout(L, best->MC, simplified);
   const size_t gbytes = ml.warp_bytes;
   const size_t avail = static_cast<size_t>(max_smem_optin) - 16 - L.blob_bytes;
   const int warps = static_cast<int>(std::min<size_t>(kMaxWarps, avail / gbytes));

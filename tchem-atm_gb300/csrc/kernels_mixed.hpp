@@ -17,7 +17,8 @@ struct MixedConfig {
   MixedLayout ml{};
 };
 
-MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch);
+MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch,
+                         bool simplified);
 cudaError_t launch_trbdf2_mixed(const AdvanceParams& P, const MechLayout& L, int grid, int warps_per_block,
                                 size_t smem, int threads_per_sample, cudaStream_t stream);
 

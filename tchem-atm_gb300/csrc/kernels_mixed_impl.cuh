@@ -40,15 +40,17 @@ namespace mixed {
 __host__ __device__ constexpr int ldu_for(int MC) { return (MC % 8 == 4) ? MC : MC + 4; }
 
 // Stage vectors kept in shared memory (FP64, [kVec][m]).
-enum Vec { V_FN = 0, V_FG = 1, V_F1 = 2, V_ATOL = 3, V_RTOL = 4, V_EST = 5, kVec = 6 };
+// V_YP / V_YGP: y_n and y_gamma of the last accepted step (simplified form's stage-1 predictor).
+enum Vec { V_FN = 0, V_FG = 1, V_YP = 2, V_ATOL = 3, V_RTOL = 4, V_YGP = 5, kVec = 6 };
 // Work counters kept in shared memory, in tchem_gb_sample_stats order.
 enum Stat { S_STEPS = 0, S_REJ = 1, S_NFAIL = 2, S_NEWTON = 3, S_LU = 4, S_SOLVE = 5, S_RHS = 6, S_JAC = 7 };
 
-inline MixedLayout make_layout(const MechLayout& L, int MC) {
+inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified) {
   auto up16 = [](size_t b) { return static_cast<uint32_t>((b + 15) & ~size_t(15)); };
   MixedLayout ml{};
   ml.LDU = ldu_for(MC);
   ml.LDL = L.m | 1;
+  ml.simplified = simplified ? 1 : 0;
   uint32_t o = 0;
   ml.x = o; o += up16(sizeof(double) * L.m);
   ml.keff = o; o += up16(sizeof(double) * L.R);
@@ -58,10 +60,11 @@ inline MixedLayout make_layout(const MechLayout& L, int MC) {
   ml.keff32 = o; o += up16(sizeof(float) * L.R);
   ml.d32 = o; o += up16(sizeof(float) * (L.NF + 1));  // d32[NF] = 0 is the padding target
   ml.ustage = o; o += up16(sizeof(float) * static_cast<size_t>(L.m) * ml.LDU);
-  ml.lrow = o; o += up16(sizeof(float) * static_cast<size_t>(L.m) * ml.LDL);
+  ml.lrow = o;  // L factor by row (LU forms only)
+  if (!simplified) o += up16(sizeof(float) * static_cast<size_t>(L.m) * ml.LDL);
   ml.pinv = o; o += up16(sizeof(float) * L.m);
   ml.piv = o; o += up16(sizeof(int) * L.m);
-  ml.ybuf = o; o += up16(sizeof(float) * L.m);
+  ml.ybuf = o; o += up16(sizeof(float) * MC);  // MC >= m
   ml.stats = o; o += up16(sizeof(int) * 8);
   ml.item = o; o += up16(sizeof(int) * 4);
   ml.warp_bytes = o;
@@ -80,6 +83,10 @@ struct Solver {
 
   float A[RPT][MC];  // active rows, shifted: register j holds column k + j at step k
   int step[RPT];     // step at which the row became the pivot (INT_MAX while active)
+  // simplified-Newton form: the stored inverse is valid / was formed in the current stage, and
+  // the coefficient c it was formed with
+  bool have_inv = false, fresh = false;
+  double c_inv = 0.0;
 
   __device__ __forceinline__ int m() const { return P.mech.L.m; }
   __device__ __forceinline__ int row(int s) const { return lane + 32 * s; }
@@ -242,8 +249,10 @@ struct Solver {
 
   // Rank-1 update with a one-column shift on groups [G0, G1): new A[j] = A[j+1] - l * U(k, k+1+j).
   // All of the chunk's U loads are issued before its FMAs.
+  // ext: the value shifted into the last register (0 for the LU; the new inverse column for
+  // Gauss-Jordan).
   template <int G0, int G1>
-  __device__ __forceinline__ void update_chunk(const float (&l)[RPT], const float* urow) {
+  __device__ __forceinline__ void update_chunk(const float (&l)[RPT], const float* urow, const float (&ext)[RPT]) {
     float4 u[G1 - G0];
 #pragma unroll
     for (int g = G0; g < G1; ++g) u[g - G0] = reinterpret_cast<const float4*>(urow)[g];
@@ -254,7 +263,7 @@ struct Solver {
         A[s][4 * g] = fmaf(-l[s], u[g - G0].x, A[s][4 * g + 1]);
         A[s][4 * g + 1] = fmaf(-l[s], u[g - G0].y, A[s][4 * g + 2]);
         A[s][4 * g + 2] = fmaf(-l[s], u[g - G0].z, A[s][4 * g + 3]);
-        A[s][4 * g + 3] = fmaf(-l[s], u[g - G0].w, (4 * g + 4 < MC) ? A[s][4 * g + 4] : 0.f);
+        A[s][4 * g + 3] = fmaf(-l[s], u[g - G0].w, (4 * g + 4 < MC) ? A[s][4 * g + 4] : ext[s]);
       }
     }
   }
@@ -270,6 +279,30 @@ struct Solver {
       key = max(key, act[s] ? kb : 0u);
     }
     return key;
+  }
+
+  // The owner lane stores registers 1..MC-1 of its row in slot pslot, then a 0, at urow (MC
+  // floats, 16-byte aligned) with predicated vector stores; no branch on the owner.
+  __device__ __forceinline__ void publish_row(float* urow, int pslot, bool is_owner) const {
+    constexpr int NG = MC / 4;
+    const uint32_t ua = static_cast<uint32_t>(__cvta_generic_to_shared(urow));
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      float v[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = 4 * g + q + 1;
+        v[q] = j < MC ? A[0][j] : 0.f;
+#pragma unroll
+        for (int s = 1; s < RPT; ++s)
+          if (pslot == s) v[q] = j < MC ? A[s][j] : 0.f;
+      }
+      asm volatile(
+          "{\n .reg .pred p;\n setp.ne.b32 p, %0, 0;\n @p st.shared.v4.f32 [%1], {%2, %3, %4, %5};\n}\n" ::"r"(
+              static_cast<int>(is_owner)),
+          "r"(ua + 16u * g), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
+          : "memory");
+    }
   }
 
   // ---- LU with the forward substitution of wf fused in --------------------------------------
@@ -309,24 +342,7 @@ struct Solver {
         if (pslot == s) { pv_mine = A[s][0]; w_mine = wf[s]; }
       // publish the pivot row's U part (registers 1..MC-1) with predicated stores
       float* urow = ustage + k * LDU;
-      const uint32_t ua = static_cast<uint32_t>(__cvta_generic_to_shared(urow));
-#pragma unroll
-      for (int g = 0; g < NG; ++g) {
-        float v[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int j = 4 * g + q + 1;
-          v[q] = j < MC ? A[0][j] : 0.f;
-#pragma unroll
-          for (int s = 1; s < RPT; ++s)
-            if (pslot == s) v[q] = j < MC ? A[s][j] : 0.f;
-        }
-        asm volatile(
-            "{\n .reg .pred p;\n setp.ne.b32 p, %0, 0;\n @p st.shared.v4.f32 [%1], {%2, %3, %4, %5};\n}\n" ::"r"(
-                static_cast<int>(is_owner)),
-            "r"(ua + 16u * g), "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
-            : "memory");
-      }
+      publish_row(urow, pslot, is_owner);
       const float pval = __shfl_sync(kFullMask, pv_mine, owner);
       const float yk = __shfl_sync(kFullMask, w_mine, owner);
       const float pinv = __fdividef(1.f, pval);
@@ -351,18 +367,134 @@ struct Solver {
       __syncwarp();
       // first group (holds the next pivot column), then the next step's pivot reduction, then
       // the rest of the update
-      update_chunk<0, 1>(l, urow);
+      const float zero[RPT] = {};
+      update_chunk<0, 1>(l, urow, zero);
       gk = __reduce_max_sync(kFullMask, pivot_key(act));
       const int width = mm - 1 - k;
-      update_chunk<1, C1>(l, urow);
+      update_chunk<1, C1>(l, urow, zero);
       if (4 * C1 < width) {
-        update_chunk<C1, C2>(l, urow);
-        if (4 * C2 < width) update_chunk<C2, NG>(l, urow);
+        update_chunk<C1, C2>(l, urow, zero);
+        if (4 * C2 < width) update_chunk<C2, NG>(l, urow, zero);
       }
       __syncwarp();
     }
     count(S_LU);
     return true;
+  }
+
+
+  // ---- Gauss-Jordan inverse (simplified-Newton form) ---------------------------------------
+  // In-place Gauss-Jordan with implicit partial pivoting on the register rows (Gauss-Jordan
+  // elimination with partial pivoting; e.g. Golub & Van Loan, Matrix Computations, 3.1 and
+  // 3.4). Column k is eliminated at step k from the not-yet-used row of largest |A(:,k)|; every
+  // other row is updated with l = A(r,k) / pivot, and the eliminated column is replaced by the
+  // inverse's column k (-l, and 1 in the pivot row), shifted in at the end of the rotating
+  // register window. Pivot rows keep their unscaled values; every later update preserves that
+  // row's scale, so each row is multiplied by its pivot's reciprocal once at the end. After m
+  // steps, register j of the row pivoted at step i holds inverse(i, p_(j - (MC - m))) where
+  // p_k is the row pivoted at step k (registers below MC - m hold zeros). The rows are stored
+  // to ustage (row-major by physical row) for apply_inverse. Returns false on a zero or
+  // non-finite pivot.
+  __device__ __forceinline__ bool invert() {
+    static_assert(32 * RPT <= 64, "row index must fit the 6 key bits");
+    constexpr int NG = MC / 4;
+    const int mm = m();
+    float* ustage = w<float>(P.ml.ustage);
+    bool act[RPT];
+    float pr[RPT];
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) {
+      act[s] = row(s) < mm;
+      step[s] = INT_MAX;
+      pr[s] = 0.f;
+    }
+    uint32_t gk = __reduce_max_sync(kFullMask, pivot_key(act));
+#pragma unroll 1
+    for (int k = 0; k < mm; ++k) {
+      if ((gk >> 6) == 0u || (gk & ~63u) >= 0x7f800000u) return false;  // zero column, inf or nan
+      const int p = 63 - static_cast<int>(gk & 63u);
+      const int owner = p & 31, pslot = p >> 5;
+      const bool is_owner = lane == owner;
+      float pv_mine = A[0][0];
+#pragma unroll
+      for (int s = 1; s < RPT; ++s)
+        if (pslot == s) pv_mine = A[s][0];
+      float* urow = ustage + k * LDU;
+      publish_row(urow, pslot, is_owner);
+      const float pinv = __fdividef(1.f, __shfl_sync(kFullMask, pv_mine, owner));
+      float l[RPT], ext[RPT];
+#pragma unroll
+      for (int s = 0; s < RPT; ++s) {
+        const bool piv_row = row(s) == p;
+        if (piv_row) {
+          act[s] = false;
+          step[s] = k;
+          pr[s] = pinv;
+        }
+        l[s] = piv_row ? 0.f : A[s][0] * pinv;
+        ext[s] = piv_row ? 1.f : -l[s];
+      }
+      __syncwarp();
+      update_chunk<0, 1>(l, urow, ext);
+      gk = __reduce_max_sync(kFullMask, pivot_key(act));
+      update_chunk<1, NG>(l, urow, ext);
+      __syncwarp();
+    }
+    // scaled rows to ustage (the pivot-row copies above are no longer needed)
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) {
+      if (row(s) < mm) {
+        float4* dst = reinterpret_cast<float4*>(ustage + row(s) * LDU);
+#pragma unroll
+        for (int g = 0; g < NG; ++g)
+          dst[g] = make_float4(A[s][4 * g] * pr[s], A[s][4 * g + 1] * pr[s], A[s][4 * g + 2] * pr[s],
+                               A[s][4 * g + 3] * pr[s]);
+      }
+    }
+    __syncwarp();
+    count(S_LU);
+    return true;
+  }
+
+  // x = A^{-1} g with the stored Gauss-Jordan inverse (g, x by row). ybuf holds g in step order
+  // after MC - m leading zeros; pinv is reused as the step-ordered result buffer.
+  __device__ __forceinline__ void apply_inverse(const float (&gf)[RPT], double (&x)[RPT]) {
+    constexpr int NG = MC / 4;
+    const int mm = m();
+    const int off = MC - mm;
+    float* gs = w<float>(P.ml.ybuf);
+    float* xs = w<float>(P.ml.pinv);
+    const float* inv = w<float>(P.ml.ustage);
+#pragma unroll
+    for (int s = 0; s < RPT; ++s)
+      if (row(s) < mm) gs[off + step[s]] = gf[s];
+    __syncwarp();
+    float a0[RPT], a1[RPT], a2[RPT], a3[RPT];
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) a0[s] = a1[s] = a2[s] = a3[s] = 0.f;
+#pragma unroll
+    for (int g = 0; g < NG; ++g) {
+      const float4 gv = reinterpret_cast<const float4*>(gs)[g];
+#pragma unroll
+      for (int s = 0; s < RPT; ++s) {
+        if (row(s) < mm) {
+          const float4 av = reinterpret_cast<const float4*>(inv + row(s) * LDU)[g];
+          a0[s] = fmaf(av.x, gv.x, a0[s]);
+          a1[s] = fmaf(av.y, gv.y, a1[s]);
+          a2[s] = fmaf(av.z, gv.z, a2[s]);
+          a3[s] = fmaf(av.w, gv.w, a3[s]);
+        }
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < RPT; ++s)
+      if (row(s) < mm) xs[step[s]] = (a0[s] + a1[s]) + (a2[s] + a3[s]);
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) x[s] = row(s) < mm ? static_cast<double>(xs[row(s)]) : 0.0;
+    __syncwarp();
+    count(S_SOLVE);
   }
 
   // Forward substitution with the stored multipliers (rows' values in wf, in place); leaves the
@@ -457,6 +589,53 @@ struct Solver {
     return false;
   }
 
+  // ---- simplified Newton on y - coef f(y) = rhs with the stored inverse --------------------
+  // The inverse of I - c_inv J (carried, or formed here at the first iterate) serves every
+  // iteration; it is re-formed once per stage at the current iterate when the max-norm of the
+  // correction (rounded to FP32) shrinks by less than half. Converged when every
+  // |dx_i| <= atol / sqrt(m) + rtol |y_i|, which implies the reference's 2-norm test
+  // (||dx|| <= atol + rtol ||y||, Minkowski's inequality); no FP64 reduction, division or square
+  // root per iteration.
+  __device__ __forceinline__ bool newton_simplified(double (&y)[RPT], const double (&rv)[RPT], double coef,
+                                                    int max_newton, double atol_c, double rtol) {
+    float prev = 0.f;
+    bool refresh = !have_inv;
+    for (int it = 0; it < max_newton; ++it) {
+      double f[RPT], dx[RPT];
+      float wf[RPT];
+      rhs(y, f);
+#pragma unroll
+      for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(-((y[s] - coef * f[s]) - rv[s]));
+      if (refresh) {
+        newton_matrix(y, coef);
+        if (!invert()) return false;
+        have_inv = true;
+        fresh = true;
+        refresh = false;
+        c_inv = coef;
+      }
+      apply_inverse(wf, dx);
+      count(S_NEWTON);
+      bool finite = true, conv = true;
+      uint32_t dbits = 0u;  // |dx| rounded to FP32: non-negative floats order like their bits
+#pragma unroll
+      for (int s = 0; s < RPT; ++s) {
+        if (row(s) < m()) {
+          y[s] += dx[s];
+          finite = finite && isfinite(dx[s]) && isfinite(y[s]);
+          conv = conv && fabs(dx[s]) <= atol_c + rtol * fabs(y[s]);
+          dbits = max(dbits, __float_as_uint(static_cast<float>(fabs(dx[s]))));
+        }
+      }
+      if (!__all_sync(kFullMask, finite)) return false;
+      const float dmax = __uint_as_float(__reduce_max_sync(kFullMask, dbits));
+      if (it > 0 && !fresh && dmax > 0.5f * prev) refresh = true;
+      prev = dmax;
+      if (__all_sync(kFullMask, conv)) return true;
+    }
+    return false;
+  }
+
   // Stores a row-distributed vector into the shared stage-vector slot v.
   __device__ __forceinline__ void put(int v, const double (&a)[RPT]) const {
 #pragma unroll
@@ -477,6 +656,9 @@ struct Solver {
     const double e0 = 1.0 / gamma, e1 = -1.0 / (gamma * (1.0 - gamma)), e2 = 1.0 / (1.0 - gamma);
     double yg[RPT], y1[RPT];
     double t = t_beg, dt = dt_in;
+    double dtp = 0.0;  // simplified form: last accepted step size (V_YP / V_YGP valid when have_prev)
+    bool have_prev = false;
+    const double natol_c = natol / sqrt(static_cast<double>(m()));
     int status = TCHEM_GB_SAMPLE_OK;
     {
       double fn[RPT];
@@ -491,6 +673,11 @@ struct Solver {
         if (last) dt = t_end - t;
         if (!(dt > 0.0)) { status = TCHEM_GB_SAMPLE_DT_UNDERFLOW; break; }
         const double coef = d * dt;
+        const bool simp = P.ml.simplified != 0;
+        if (simp) {
+          // keep the carried inverse while c moved by at most 30%
+          if (!(have_inv && fabs(coef / c_inv - 1.0) <= 0.3)) have_inv = false;
+        }
         // Both implicit stages run through one copy of the Newton code.
         bool ok = true;
 #pragma unroll 1
@@ -502,7 +689,32 @@ struct Solver {
             rv[s] = stage == 0 ? y[s] + coef * vec(V_FN, i) : cg * yg[s] - cn * y[s];
             guess[s] = stage == 0 ? y[s] : yg[s];
           }
-          ok = newton(guess, rv, coef, max_newton, jac_interval, natol, nrtol);
+          if (simp) {
+            if (stage == 0 && have_prev) {
+              // stage-1 guess: the quadratic through the last step's y_{n-1}, y_{n-1+gamma}, y_n
+              const double t0 = -dtp, t1 = -(1.0 - gamma) * dtp, tt = gamma * dt;
+              const double l0 = (tt - t1) * tt / ((t0 - t1) * t0);
+              const double l1 = (tt - t0) * tt / ((t1 - t0) * t1);
+              const double l2 = (tt - t0) * (tt - t1) / (t0 * t1);
+#pragma unroll
+              for (int s = 0; s < RPT; ++s) {
+                const int i = row(s) < m() ? row(s) : 0;
+                guess[s] = l0 * vec(V_YP, i) + l1 * vec(V_YGP, i) + l2 * y[s];
+              }
+            } else if (stage == 1) {
+              // stage-2 guess: the quadratic with p(t) = y_n, p'(t) = f_n, p(t + gamma dt) = y_gamma
+              const double a = 1.0 / (gamma * gamma), b = dt * (1.0 - 1.0 / gamma);
+#pragma unroll
+              for (int s = 0; s < RPT; ++s) {
+                const int i = row(s) < m() ? row(s) : 0;
+                guess[s] = (1.0 - a) * y[s] + a * yg[s] + b * vec(V_FN, i);
+              }
+            }
+            fresh = false;
+            ok = newton_simplified(guess, rv, coef, max_newton, natol_c, nrtol);
+          } else {
+            ok = newton(guess, rv, coef, max_newton, jac_interval, natol, nrtol);
+          }
           if (ok) {
 #pragma unroll
             for (int s = 0; s < RPT; ++s) {
@@ -534,8 +746,22 @@ struct Solver {
         float wf[RPT];
 #pragma unroll
         for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(est[s]);
-        forward(wf);
-        backward(estf);
+        if (P.ml.simplified) {
+          // filter with I - c J(y_{n+1}); the inverse is carried into the next step
+          newton_matrix(y1, d * dt);
+          if (invert()) {
+            have_inv = true;
+            c_inv = d * dt;
+            apply_inverse(wf, estf);
+          } else {
+            have_inv = false;
+#pragma unroll
+            for (int s = 0; s < RPT; ++s) estf[s] = __longlong_as_double(0x7ff8000000000000ll);  // NaN: status 4
+          }
+        } else {
+          forward(wf);
+          backward(estf);
+        }
       }
       double err = 0.0;
 #pragma unroll
@@ -549,6 +775,12 @@ struct Solver {
       if (!isfinite(err)) { status = TCHEM_GB_SAMPLE_NONFINITE; break; }
       if (err <= 1.0 || dt <= dt_min) {
         t = last ? t_end : t + dt;
+        if (P.ml.simplified) {
+          put(V_YP, y);
+          put(V_YGP, yg);
+          dtp = dt;
+          have_prev = true;
+        }
 #pragma unroll
         for (int s = 0; s < RPT; ++s) y[s] = y1[s];
         put(V_FN, f1);
@@ -638,6 +870,9 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
       S.template w<double>(P.ml.q)[L.R] = 0.0;
       S.template w<float>(P.ml.d32)[L.NF] = 0.f;
     }
+    if (P.ml.simplified)
+      for (int j = lane; j < MC; j += 32) S.template w<float>(P.ml.ybuf)[j] = 0.f;  // leading zeros of apply_inverse
+    S.have_inv = false;
     __syncwarp();
     double y[RPT];
 #pragma unroll

@@ -18,7 +18,7 @@ import numpy as np
 from . import _capi
 from .mechanism import KineticModel
 
-FORMS = {"plain": 0, "fp64": 0, "mixed": 1}
+FORMS = {"plain": 0, "fp64": 0, "mixed": 1, "simplified": 2, "mixed_simplified": 2}
 
 
 AdvanceOpts = _capi.AdvanceOpts

@@ -230,23 +230,44 @@ def test_per_sample_mechanisms_match_oracle():
     assert st_bad[5] == 6 and np.all(np.delete(st_bad, 5) == 0)
 
 
-# --- mixed-precision form ---------------------------------------------------------------------------
+# --- mixed-precision forms ---------------------------------------------------------------------------
 
-def test_mixed_matches_fp64_oracle_on_cb05_shaped_batch(cfg1_like):
+MIXED_FORMS = ["mixed", "simplified"]
+
+
+@pytest.mark.parametrize("form", MIXED_FORMS)
+def test_mixed_matches_fp64_oracle_on_cb05_shaped_batch(cfg1_like, form):
     km, state, tadv, tol_time, ref = cfg1_like
-    out, t, dt, st, stats = gpu_advance(km, tadv, state, [1e-18, 1e-8], tol_time, form="mixed", stats=True)
+    out, t, dt, st, stats = gpu_advance(km, tadv, state, [1e-18, 1e-8], tol_time, form=form, stats=True)
     m = km.n_active
     assert np.all(st == 0)
     assert np.all(t == 3600.0) and np.all(dt == 0.0)
     err = rel_error(out[:, 3:3 + m], ref[0][:, 3:3 + m], ATOL_TIME)
     assert err.max() <= 1e-6, err.max()
     np.testing.assert_array_equal(out[:, :3], state[:, :3])
-    # The FP32 LU does not change the step-size sequence much: mean steps within 1 %.
+    # Neither the FP32 linear algebra nor the simplified Newton changes the step-size sequence
+    # much: mean steps within 1 %.
     assert abs(stats[:, 0].mean() / ref[4]["n_steps"].mean() - 1.0) < 0.01
 
 
+def test_simplified_form_follows_its_oracle_restatement(cfg1_like):
+    """The engine's simplified form (Gauss-Jordan inverse) against the oracle's simplified form
+    (FP32 LU): same end states to the Newton tolerance and the same work counts within a few %."""
+    km, state, tadv, tol_time, _ = cfg1_like
+    B = 64
+    ref = Oracle([km]).time_advance(tadv[:B], state[:B], [1e-18, 1e-8], tol_time, lu_fp32=1, simplified=True)
+    out, t, dt, st, stats = gpu_advance(km, tadv[:B], state[:B], [1e-18, 1e-8], tol_time, form="simplified",
+                                        stats=True)
+    m = km.n_active
+    np.testing.assert_array_equal(st, ref[3])
+    assert rel_error(out[:, 3:3 + m], ref[0][:, 3:3 + m], ATOL_TIME).max() <= 1e-7
+    for col, name in [(0, "n_steps"), (3, "n_newton_iter"), (4, "n_lu")]:
+        assert abs(stats[:, col].mean() / ref[4][name].mean() - 1.0) < 0.03, name
+
+
+@pytest.mark.parametrize("form", MIXED_FORMS)
 @pytest.mark.parametrize("tps", [0, 32])
-def test_mixed_threads_per_sample_shapes_agree(cb05, tps):
+def test_mixed_threads_per_sample_shapes_agree(cb05, tps, form):
     km, state, tadv, tol_time = generated_case(24, seed=31, horizon=600.0, km=cb05)
     ref = Oracle([km]).time_advance(tadv, state, [1e-18, 1e-8], tol_time)
     d_state = _dev(state)
@@ -254,7 +275,7 @@ def test_mixed_threads_per_sample_shapes_agree(cb05, tps):
     d_t = torch.zeros(24, dtype=torch.float64, device="cuda")
     d_dt = torch.zeros_like(d_t)
     st = AtmosphericChemistry.runDeviceBatch(_dev([1e-18, 1e-8]), _dev(tol_time), None, tadv_to_device(tadv), d_state,
-                                             d_t, d_dt, d_out, km, form="mixed", threads_per_sample=tps)
+                                             d_t, d_dt, d_out, km, form=form, threads_per_sample=tps)
     torch.cuda.synchronize()
     assert int((st != 0).sum()) == 0
     m = km.n_active
@@ -262,7 +283,8 @@ def test_mixed_threads_per_sample_shapes_agree(cb05, tps):
     assert err.max() <= 1e-6
 
 
-def test_mixed_per_sample_mechanisms_and_edge_cases():
+@pytest.mark.parametrize("form", MIXED_FORMS)
+def test_mixed_per_sample_mechanisms_and_edge_cases(form):
     day = KineticModel.from_string(mechanism_yaml(MechanismSpec()))
     night = KineticModel.from_string(mechanism_yaml(MechanismSpec(), night=True))
     small = KineticModel.from_string(mechanism_yaml(MechanismSpec(n_species=20, n_reactions=60, seed=99)))
@@ -284,7 +306,7 @@ def test_mixed_per_sample_mechanisms_and_edge_cases():
     tadv["dt"][7] = -1.0    # negative dt_in
     tol_time = np.tile([ATOL_TIME, 1e-6], (day.n_active, 1))
     ref = Oracle(mechs).time_advance(tadv, state, [1e-18, 1e-8], tol_time, t_out=t_in, mech_of_sample=mos)
-    out, t, dt, st, _ = gpu_advance(mechs, tadv, state, [1e-18, 1e-8], tol_time, t_out=t_in, form="mixed",
+    out, t, dt, st, _ = gpu_advance(mechs, tadv, state, [1e-18, 1e-8], tol_time, t_out=t_in, form=form,
                                     mech_of_sample=mos)
     np.testing.assert_array_equal(st, ref[3])
     assert st[4] == 2 and st[7] == 3
@@ -295,6 +317,6 @@ def test_mixed_per_sample_mechanisms_and_edge_cases():
         n = (small if mos[b] == 2 else day).n_active
         assert rel_error(out[b, 3:3 + n], ref[0][b, 3:3 + n], ATOL_TIME).max() <= 1e-6, b
     # Newton failure convention in the mixed form too.
-    out3, t3, dt3, st3, _ = gpu_advance(day, tadv[:3], big[:3], [-1.0, 0.0], tol_time, form="mixed")
+    out3, t3, dt3, st3, _ = gpu_advance(day, tadv[:3], big[:3], [-1.0, 0.0], tol_time, form=form)
     assert np.all(st3 == 1) and np.all(t3 == 600.0) and np.all(dt3 == -1.0)
     assert np.all(out3[:, 3:3 + day.n_active] == 0.0)

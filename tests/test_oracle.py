@@ -149,6 +149,24 @@ def test_fp32_lu_mode_tracks_fp64():
     assert err.max() < 1e-5
 
 
+@pytest.mark.parametrize("lu_fp32", [0, 1])
+def test_simplified_newton_mode_tracks_fp64(lu_fp32):
+    """Carried factors, componentwise Newton test and the filter at I - c J(y_{n+1}): end states
+    within 1e-6 of the full-Newton FP64 run, with the same step sequence and about a quarter of
+    the factorizations."""
+    km, state, tadv, tol_time = _generated_batch(16, seed=21)
+    o = Oracle([km])
+    a = o.time_advance(tadv, state, [1e-18, 1e-8], tol_time)
+    b = o.time_advance(tadv, state, [1e-18, 1e-8], tol_time, lu_fp32=lu_fp32, simplified=True)
+    m = km.n_active
+    assert np.all(b[3] == 0) and np.all(b[1] == 3600.0)
+    assert rel_error(b[0][:, 3:3 + m], a[0][:, 3:3 + m], 1e-12).max() <= 1e-6
+    assert abs(b[4]["n_steps"].mean() / a[4]["n_steps"].mean() - 1.0) < 0.01
+    assert b[4]["n_lu"].sum() < 0.35 * a[4]["n_lu"].sum()
+    # every accepted step formed the filter factors once
+    assert np.all(b[4]["n_lu"] >= b[4]["n_steps"])
+
+
 def test_failure_conventions():
     km, state, tadv, tol_time = _generated_batch(3)
     o = Oracle([km])
