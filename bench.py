@@ -1,0 +1,426 @@
+#!/usr/bin/env python3
+"""Benchmark of the batched box-model TR-BDF2 time advance (TChem::AtmosphericChemistry::runDeviceBatch).
+
+Workload (one "step"): advance every sample of the CB05-shaped batch -- 51 active species, one
+constant species, 156 reactions (60 % Arrhenius, 10 % Troe, 30 % fixed-J photolysis), seeded --
+from t = 0 to the 3600 s horizon with adaptive TR-BDF2 steps (dt_in = dt_min = 1e-10, dt_max =
+3600, atol 1e-12, rtol 1e-6, Newton 1e-18 / 1e-8, at most 20 Newton iterations). The batch is
+1,048,576 samples per GPU with T ~ U[260, 310] K, p ~ U[0.8, 1.05] atm and number densities
+log-uniform in [1e2, 1e12] cm^-3 (synthetic, seeded). The state array (1,048,576 x 55 doubles,
+461 MB) is larger than L2, so no flush is needed between steps.
+
+Metric: box-samples/s = samples advanced to the horizon per second (whole job, all ranks).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference] [--form simplified]
+
+--impl engine (default) times the engine's chosen form through the device API (value), then one
+end-to-end pass through the host-buffer C ABI with host<->device copies inside the timed region
+(e2e), the plain FP64 form on a subsample, the CPU oracle on a bounded subsample (cpu_baseline)
+and the end-state error of the chosen form against the FP64 results.
+--impl reference times the reference algorithm's CPU restatement (the oracle, FP64, OpenMP on all
+host threads) on a bounded subsample per step; the reference's own Kokkos build cannot be built
+here (Kokkos, Tines, Sacado and yaml-cpp are absent).
+Under torchrun each rank advances its own batch (samples are independent: weak scaling, no
+collective on the data path); the time is the max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+for _p in (ROOT, ROOT / "tchem-atm_gb300"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+from tchem_gb import _capi  # noqa: E402
+from tchem_gb.generator import MechanismSpec, mechanism_yaml, sample_states  # noqa: E402
+from tchem_gb.mechanism import KineticModel  # noqa: E402
+
+METRIC = "box-samples/s"
+HORIZON = 3600.0
+TOL_NEWTON = (1e-18, 1e-8)
+ATOL, RTOL = 1e-12, 1e-6
+SEED = 7
+# Form names of the C ABI's tchem_gb_form.
+FORM_DTYPE = {"plain": "f64", "mixed": "f64 state / f32 LU", "simplified": "f64 state / f32 Gauss-Jordan inverse"}
+# DRAM bytes per sample of the simplified-form kernel, from one ncu capture of a 4096-sample,
+# 600 s case (profiles/trbdf2_simplified_cb05_4096.md): the per-sample traffic (state in and out,
+# time-advance record, statistics) does not depend on the horizon.
+NCU_DRAM_BYTES_PER_SAMPLE = None
+
+
+def parse() -> argparse.Namespace:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
+    ap.add_argument("--form", choices=["simplified", "mixed", "plain"], default="simplified")
+    ap.add_argument("--samples", type=int, default=1 << 20, help="samples per GPU (the workload is 1,048,576)")
+    ap.add_argument("--plain-samples", type=int, default=4096, help="subsample for the plain FP64 form")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of one oracle sample")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+# ---- workload ---------------------------------------------------------------------------------
+
+def workload(B: int, rank: int):
+    km = KineticModel.from_string(mechanism_yaml(MechanismSpec()))
+    m = km.n_active
+    state = sample_states(B, m, seed=SEED + rank)
+    tadv = np.zeros(B, dtype=_capi.TIME_ADVANCE_DTYPE)
+    tadv["tbeg"], tadv["tend"], tadv["dt"], tadv["dtmin"], tadv["dtmax"] = 0.0, HORIZON, 1e-10, 1e-10, HORIZON
+    tadv["max_num_newton_iterations"] = 20
+    tadv["num_time_iterations_per_interval"] = 1_000_000
+    tadv["jacobian_interval"] = 1
+    tol_time = np.tile([ATOL, RTOL], (m, 1))
+    return km, state, tadv, tol_time
+
+
+def flops_per_call(km) -> tuple[float, float, float]:
+    """Algorithmic flops of one RHS, one analytic Jacobian and one factorization (m^3 * 2/3)."""
+    v = km.view
+    R, S = v.nReac, v.maxSpecInReac
+    nr = np.ctypeslib.as_array(v.reacNreac, (R,))
+    npd = np.ctypeslib.as_array(v.reacNprod, (R,))
+    nu = np.ctypeslib.as_array(v.reacNuki, (R * S,)).reshape(R, S)
+    nu_reac = np.array([np.abs(nu[r, :nr[r]]).sum() for r in range(R)])
+    f_rhs = float(np.sum(2 * nu_reac + 2 * (nr + npd)))
+    f_jac = float(np.sum(nr * (2 * nr + 2 * (nr + npd))))
+    m = km.n_active
+    return f_rhs, f_jac, 2.0 / 3.0 * m ** 3
+
+
+def work_flops(km, stats: np.ndarray) -> tuple[float, float]:
+    """(FP32-side, FP64-side) algorithmic flops of a run from its per-sample counters: LU and
+    solves and Jacobians are the linear-algebra side, RHS evaluations the FP64 side."""
+    f_rhs, f_jac, f_lu = flops_per_call(km)
+    m = km.n_active
+    s = stats.astype(np.float64)
+    f32 = s[:, 4].sum() * f_lu + s[:, 5].sum() * 2 * m * m + s[:, 7].sum() * f_jac
+    f64 = s[:, 6].sum() * f_rhs
+    return f32, f64
+
+
+# ---- clocks -----------------------------------------------------------------------------------
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=10)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+        return False
+
+    def summary(self) -> dict:
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---- distributed helpers ----------------------------------------------------------------------
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group(backend="nccl" if n_gpus > 0 else "gloo")
+    return world, rank, local
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int, device) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---- CPU legs (the oracle is the checker and the CPU restatement) -------------------------------
+
+def cpu_sample_size(km, state, tadv, tol_time, seconds: float) -> tuple[int, float]:
+    """Samples of the CPU oracle that take about `seconds` on all host threads."""
+    from oracle import Oracle
+    o = Oracle([km])
+    n0 = max(2 * (os.cpu_count() or 1), 16)
+    t0 = time.perf_counter()
+    o.time_advance(tadv[:n0], state[:n0], TOL_NEWTON, tol_time)
+    rate = n0 / (time.perf_counter() - t0)
+    n = int(max(n0, min(len(state), rate * seconds)))
+    return n, rate
+
+
+def run_oracle(km, state, tadv, tol_time, n: int):
+    from oracle import Oracle
+    t0 = time.perf_counter()
+    res = Oracle([km]).time_advance(tadv[:n], state[:n], TOL_NEWTON, tol_time)
+    return res, time.perf_counter() - t0
+
+
+def bench_config(B: int, form: str, world: int) -> dict:
+    """The workload description shared by both arms."""
+    return {"workload": f"cb05-shaped 51 species / 156 reactions, {B} samples per GPU, 3600 s TR-BDF2",
+            "samples_per_gpu": B, "horizon_s": HORIZON, "form": form, "parallelism": f"replicas x{world}",
+            "l2": "inputs larger than L2 (461 MB state per GPU); no flush"}
+
+
+def rel_err(test: np.ndarray, ref: np.ndarray) -> np.ndarray:
+    """Per-sample max over species of |test - ref| / max(|ref|, atol)."""
+    return (np.abs(test - ref) / np.maximum(np.abs(ref), ATOL)).max(axis=1)
+
+
+# ---- reference arm ----------------------------------------------------------------------------
+
+def reference_arm(args, world: int, rank: int):
+    if rank != 0:
+        return  # one CPU measurement per node; the other ranks have no work
+    km, state, tadv, tol_time = workload(max(args.samples, 1), 0)
+    n, _ = cpu_sample_size(km, state, tadv, tol_time, args.cpu_seconds)
+    for _ in range(args.warmup):
+        run_oracle(km, state, tadv, tol_time, n)
+    total = 0.0
+    for _ in range(args.steps):
+        _, el = run_oracle(km, state, tadv, tol_time, n)
+        total += el
+    value = n * args.steps / total
+    cores = os.cpu_count() or 1
+    sample = (f"first {n} of the {args.samples}-sample CB05-shaped batch per step (FP64 TR-BDF2 CPU restatement, "
+              f"OpenMP dynamic over samples on {cores} threads); samples are independent, so box-samples/s "
+              f"of the full batch equals this rate")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": bench_config(args.samples, args.form, world),
+        "cpu_baseline": {"value": value, "unit": "samples/s", "cores": cores, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "samples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference's Kokkos/Tines build is unavailable here (submodules absent, no network); the "
+                "oracle restatement of its algorithm is timed instead",
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---- engine arm -------------------------------------------------------------------------------
+
+def engine_arm(args, world: int, rank: int, local: int):
+    import torch
+    from tchem_gb import AtmosphericChemistry, tadv_to_device
+
+    assert torch.cuda.is_available(), "the engine arm needs a CUDA device"
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    B = args.samples
+    km, state, tadv, tol_time = workload(B, rank)
+    m = km.n_active
+    stream = torch.cuda.current_stream(dev)
+
+    d_tn = torch.tensor(TOL_NEWTON, dtype=torch.float64, device=dev)
+    d_tt = torch.as_tensor(tol_time).to(dev)
+    d_tadv = tadv_to_device(tadv, dev)
+    d_state = torch.as_tensor(state).to(dev)
+    d_out = torch.empty_like(d_state)
+    d_t = torch.zeros(B, dtype=torch.float64, device=dev)
+    d_dt = torch.zeros_like(d_t)
+    d_status = torch.empty(B, dtype=torch.int32, device=dev)
+    d_stats = torch.zeros(B, 8, dtype=torch.int32, device=dev)
+    ws_bytes = AtmosphericChemistry.getWorkSpaceSize(km, B, form=args.form)
+    d_ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+
+    def step(with_stats: bool):
+        d_t.zero_()  # every sample restarts at t = 0 (samples with t >= tend are skipped)
+        AtmosphericChemistry.runDeviceBatch(d_tn, d_tt, None, d_tadv, d_state, d_t, d_dt, d_out, km,
+                                            status=d_status, stats=d_stats if with_stats else None,
+                                            form=args.form, workspace=d_ws, stream=stream)
+
+    for _ in range(args.warmup):
+        step(False)
+    torch.cuda.synchronize(dev)
+    assert AtmosphericChemistry.device_error(d_ws, stream) == 0
+
+    # timed region: K steps, CUDA events on the launching stream, barrier + sync on both sides
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    with ClockSampler(local) as clk:
+        e0.record(stream)
+        for k in range(args.steps):
+            step(k == args.steps - 1)
+        e1.record(stream)
+        torch.cuda.synchronize(dev)
+    barrier(world)
+    ms_local = e0.elapsed_time(e1)
+    ms = max_over_ranks(ms_local, world, dev)
+    value = B * world * args.steps / (ms * 1e-3)
+    status = d_status.cpu().numpy()
+    stats = d_stats.cpu().numpy()
+    out = d_out.cpu().numpy()
+    n_fail = int((status != 0).sum())
+    kernel_ms = ms_local / args.steps  # one engine kernel per step (one mechanism group)
+
+    # roofline of the time-advance kernel: algorithmic flops per launch / launch time
+    f32, f64 = work_flops(km, stats)
+    peak64, peak32 = C.c_double(), C.c_double()
+    L = _capi.lib()
+    L.tchem_gb_measure_fma_peak(1, 4, 4096, C.byref(peak64))
+    L.tchem_gb_measure_fma_peak(0, 4, 65536, C.byref(peak32))
+    ach64 = f64 / (kernel_ms * 1e-3) / 1e12
+    ach32 = f32 / (kernel_ms * 1e-3) / 1e12
+    traffic = None if NCU_DRAM_BYTES_PER_SAMPLE is None else NCU_DRAM_BYTES_PER_SAMPLE * B
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": FORM_DTYPE[args.form], "data": "synthetic (seeded CB05-shaped mechanism and states)",
+        "config": bench_config(B, args.form, world),
+        "failed_samples": n_fail,
+        "work_per_sample": {k: float(stats[:, i].mean()) for i, k in enumerate(
+            ["steps", "rejected", "newton_fail", "newton_iter", "factorizations", "solves", "rhs", "jacobians"])},
+        "gpu_launches": args.steps,
+        "clocks": clk.summary(),
+        "roofline": {"bound": "fp64", "achieved": ach64, "peak": peak64.value / 1e12, "unit": "TFLOP/s",
+                     "frac": ach64 / (peak64.value / 1e12), "traffic": traffic,
+                     "peak_source": "FMA-chain probe measured in this run (tchem_gb_measure_fma_peak); "
+                                    "MEASURED_PEAKS.json has no FP64/FP32 figure",
+                     "fp32": {"achieved": ach32, "peak": peak32.value / 1e12,
+                              "frac": ach32 / (peak32.value / 1e12)}},
+    }
+
+    if rank == 0:
+        # plain FP64 form on a subsample: its rate and the FP64 end states for the error figure
+        P = min(args.plain_samples, B)
+        if P > 0 and args.form != "plain":
+            p_out = torch.empty(P, d_state.shape[1], dtype=torch.float64, device=dev)
+            p_t = torch.zeros(P, dtype=torch.float64, device=dev)
+            p_dt = torch.zeros_like(p_t)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            st_p = AtmosphericChemistry.runDeviceBatch(d_tn, d_tt, None, d_tadv[:P], d_state[:P].contiguous(), p_t,
+                                                       p_dt, p_out, km, form="plain", stream=stream)
+            ev1.record(stream)
+            torch.cuda.synchronize(dev)
+            plain_rate = P / (ev0.elapsed_time(ev1) * 1e-3)
+            e = rel_err(out[:P, 3:3 + m], p_out.cpu().numpy()[:, 3:3 + m])
+            line["plain_fp64"] = {"value": plain_rate, "unit": "samples/s", "samples": P,
+                                  "failed_samples": int((st_p != 0).sum()),
+                                  "note": "subsample of the same batch; samples are independent"}
+            line["accuracy_vs_plain_fp64_gpu"] = {"samples": P, "max": float(e.max()),
+                                                  "p99": float(np.percentile(e, 99)), "floor": ATOL}
+        # CPU oracle: baseline rate and the accuracy reference
+        n, _ = cpu_sample_size(km, state, tadv, tol_time, args.cpu_seconds)
+        res, el = run_oracle(km, state, tadv, tol_time, n)
+        e = rel_err(out[:n, 3:3 + m], res[0][:, 3:3 + m])
+        cores = os.cpu_count() or 1
+        line["cpu_baseline"] = {"value": n / el, "unit": "samples/s", "cores": cores, "kind": "port",
+                                "sample": f"first {n} samples of the batch, FP64 TR-BDF2 CPU restatement, OpenMP "
+                                          f"over samples on {cores} threads ({el:.1f} s)"}
+        line["accuracy_vs_fp64_oracle"] = {"samples": n, "max": float(e.max()), "p99": float(np.percentile(e, 99)),
+                                           "floor": ATOL}
+
+    if not args.no_e2e:
+        # end to end through the host-buffer C ABI: pinned host arrays in, results out, every copy
+        # inside the timed region
+        h_state = torch.empty(state.shape, dtype=torch.float64, pin_memory=True).numpy()
+        h_state[:] = state
+        h_out = torch.empty(state.shape, dtype=torch.float64, pin_memory=True).numpy()
+        h_tadv = torch.empty(tadv.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(tadv.dtype)
+        h_tadv[:] = tadv
+        h_t = torch.zeros(B, dtype=torch.float64, pin_memory=True).numpy()
+        h_dt = torch.zeros(B, dtype=torch.float64, pin_memory=True).numpy()
+        h_st = torch.zeros(B, dtype=torch.int32, pin_memory=True).numpy()
+        tn = np.asarray(TOL_NEWTON, dtype=np.float64)
+        o = _capi.AdvanceOpts()
+        o.form = {"plain": 0, "mixed": 1, "simplified": 2}[args.form]
+        p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+        handles = (C.c_void_p * 1)(km.handle.value)
+        barrier(world)
+        t0 = time.perf_counter()
+        rc = L.tchem_gb_time_advance_hostbuf(handles, 1, None, B, p(tn), p(tol_time), p(h_tadv), p(h_state),
+                                             p(h_t), p(h_dt), p(h_out), p(h_st), None, C.byref(o),
+                                             C.c_void_p(stream.cuda_stream))
+        el = time.perf_counter() - t0
+        _capi.check(rc, "tchem_gb_time_advance_hostbuf")
+        el = max_over_ranks(el, world, dev)
+        dim = state.shape[1]
+        h2d = 16 + 16 * m + tadv.itemsize * B + 8 * B * dim + 8 * B
+        d2h = 8 * B * dim + 8 * B + 8 * B + 4 * B
+        line["e2e"] = {"value": B * world / el, "unit": "samples/s", "h2d_bytes_per_step": h2d,
+                       "d2h_bytes_per_step": d2h, "failed_samples": int((h_st != 0).sum()),
+                       "path": "tchem_gb_time_advance_hostbuf (C ABI, pinned host buffers)"}
+        line["gpu_launches"] = args.steps  # the e2e pass is timed separately
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    world, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        reference_arm(args, world, rank)
+    else:
+        engine_arm(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

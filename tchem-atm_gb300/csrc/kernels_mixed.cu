@@ -10,15 +10,20 @@
 
 namespace tchem_gb {
 
-// Launchers defined in kernels_mixed_v*.cu (one translation unit per kernel shape).
-cudaError_t launch_mixed_24_1(const AdvanceParams&, int, int, size_t, cudaStream_t);
-const void* kernel_mixed_24_1();
-cudaError_t launch_mixed_32_1(const AdvanceParams&, int, int, size_t, cudaStream_t);
-const void* kernel_mixed_32_1();
-cudaError_t launch_mixed_52_2(const AdvanceParams&, int, int, size_t, cudaStream_t);
-const void* kernel_mixed_52_2();
-cudaError_t launch_mixed_64_2(const AdvanceParams&, int, int, size_t, cudaStream_t);
-const void* kernel_mixed_64_2();
+// Launchers defined in kernels_mixed_v*.cu (FP32 LU) and kernels_simpl_v*.cu (simplified Newton),
+// one translation unit per kernel.
+#define TCHEM_GB_DECLARE_SHAPE(PRE, MC, RPT)                                                    \
+  cudaError_t launch_##PRE##_##MC##_##RPT(const AdvanceParams&, int, int, size_t, cudaStream_t); \
+  const void* kernel_##PRE##_##MC##_##RPT();
+TCHEM_GB_DECLARE_SHAPE(mixed, 24, 1)
+TCHEM_GB_DECLARE_SHAPE(mixed, 32, 1)
+TCHEM_GB_DECLARE_SHAPE(mixed, 52, 2)
+TCHEM_GB_DECLARE_SHAPE(mixed, 64, 2)
+TCHEM_GB_DECLARE_SHAPE(simpl, 24, 1)
+TCHEM_GB_DECLARE_SHAPE(simpl, 32, 1)
+TCHEM_GB_DECLARE_SHAPE(simpl, 52, 2)
+TCHEM_GB_DECLARE_SHAPE(simpl, 64, 2)
+#undef TCHEM_GB_DECLARE_SHAPE
 
 namespace {
 
@@ -26,28 +31,29 @@ constexpr int kMaxWarps = 8;
 
 struct Variant {
   int MC, RPT;
+  bool simplified;
   const void* kernel;
   cudaError_t (*launch)(const AdvanceParams&, int, int, size_t, cudaStream_t);
 };
 
-// Kernel shapes (columns, rows per lane); a mechanism uses the narrowest with MC >= m and
-// 32 * RPT >= m.
+// Kernel shapes (columns, rows per lane) of each form; a mechanism uses the narrowest with
+// MC >= m and 32 * RPT >= m.
 const Variant* variants(int* n) {
   static const Variant v[] = {
-      {24, 1, kernel_mixed_24_1(), &launch_mixed_24_1},
-      {32, 1, kernel_mixed_32_1(), &launch_mixed_32_1},
-      {52, 2, kernel_mixed_52_2(), &launch_mixed_52_2},
-      {64, 2, kernel_mixed_64_2(), &launch_mixed_64_2},
+      {24, 1, false, kernel_mixed_24_1(), &launch_mixed_24_1}, {32, 1, false, kernel_mixed_32_1(), &launch_mixed_32_1},
+      {52, 2, false, kernel_mixed_52_2(), &launch_mixed_52_2}, {64, 2, false, kernel_mixed_64_2(), &launch_mixed_64_2},
+      {24, 1, true, kernel_simpl_24_1(), &launch_simpl_24_1},  {32, 1, true, kernel_simpl_32_1(), &launch_simpl_32_1},
+      {52, 2, true, kernel_simpl_52_2(), &launch_simpl_52_2},  {64, 2, true, kernel_simpl_64_2(), &launch_simpl_64_2},
   };
   *n = static_cast<int>(sizeof(v) / sizeof(v[0]));
   return v;
 }
 
-const Variant* pick(const MechLayout& L) {
+const Variant* pick(const MechLayout& L, bool simplified) {
   int nv = 0;
   const Variant* v = variants(&nv);
   for (int i = 0; i < nv; ++i)
-    if (v[i].MC >= L.m && 32 * v[i].RPT >= L.m) return &v[i];
+    if (v[i].simplified == simplified && v[i].MC >= L.m && 32 * v[i].RPT >= L.m) return &v[i];
   return nullptr;
 }
 
@@ -57,7 +63,7 @@ MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_cou
                          bool simplified) {
   if (threads_per_sample != 0 && threads_per_sample != 32)
     throw std::domain_error("mixed form: threads_per_sample must be 0 or 32");
-  const Variant* best = pick(L);
+  const Variant* best = pick(L, simplified);
   if (!best) throw std::domain_error("mixed form: mechanisms with more than 64 active species are not supported");
   const MixedLayout ml = mixed::make_layout(L, best->MC, simplified);
   const size_t gbytes = ml.warp_bytes;
@@ -81,7 +87,7 @@ MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_cou
 
 cudaError_t launch_trbdf2_mixed(const AdvanceParams& P, const MechLayout& L, int grid, int warps_per_block,
                                 size_t smem, int /*threads_per_sample*/, cudaStream_t stream) {
-  const Variant* best = pick(L);
+  const Variant* best = pick(L, P.ml.simplified != 0);
   if (!best) return cudaErrorInvalidValue;
   return best->launch(P, grid, warps_per_block * 32, smem, stream);
 }

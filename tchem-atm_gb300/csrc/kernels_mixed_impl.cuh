@@ -71,7 +71,9 @@ inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified) {
   return ml;
 }
 
-template <int MC, int RPT>
+// SIMP selects the simplified-Newton form (Gauss-Jordan inverse); each form is its own kernel so
+// that neither carries the other's code through the instruction cache.
+template <int MC, int RPT, bool SIMP>
 struct Solver {
   static_assert(MC % 4 == 0, "MC must be a multiple of 4");
   static constexpr int LDU = ldu_for(MC);
@@ -437,7 +439,10 @@ struct Solver {
       __syncwarp();
       update_chunk<0, 1>(l, urow, ext);
       gk = __reduce_max_sync(kFullMask, pivot_key(act));
-      update_chunk<1, NG>(l, urow, ext);
+      constexpr int C1 = (NG + 2) / 3, C2 = (2 * NG + 2) / 3;
+      update_chunk<1, C1>(l, urow, ext);
+      update_chunk<C1, C2>(l, urow, ext);
+      update_chunk<C2, NG>(l, urow, ext);
       __syncwarp();
     }
     // scaled rows to ustage (the pivot-row copies above are no longer needed)
@@ -673,8 +678,7 @@ struct Solver {
         if (last) dt = t_end - t;
         if (!(dt > 0.0)) { status = TCHEM_GB_SAMPLE_DT_UNDERFLOW; break; }
         const double coef = d * dt;
-        const bool simp = P.ml.simplified != 0;
-        if (simp) {
+        if constexpr (SIMP) {
           // keep the carried inverse while c moved by at most 30%
           if (!(have_inv && fabs(coef / c_inv - 1.0) <= 0.3)) have_inv = false;
         }
@@ -689,7 +693,7 @@ struct Solver {
             rv[s] = stage == 0 ? y[s] + coef * vec(V_FN, i) : cg * yg[s] - cn * y[s];
             guess[s] = stage == 0 ? y[s] : yg[s];
           }
-          if (simp) {
+          if constexpr (SIMP) {
             if (stage == 0 && have_prev) {
               // stage-1 guess: the quadratic through the last step's y_{n-1}, y_{n-1+gamma}, y_n
               const double t0 = -dtp, t1 = -(1.0 - gamma) * dtp, tt = gamma * dt;
@@ -746,7 +750,7 @@ struct Solver {
         float wf[RPT];
 #pragma unroll
         for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(est[s]);
-        if (P.ml.simplified) {
+        if constexpr (SIMP) {
           // filter with I - c J(y_{n+1}); the inverse is carried into the next step
           newton_matrix(y1, d * dt);
           if (invert()) {
@@ -775,7 +779,7 @@ struct Solver {
       if (!isfinite(err)) { status = TCHEM_GB_SAMPLE_NONFINITE; break; }
       if (err <= 1.0 || dt <= dt_min) {
         t = last ? t_end : t + dt;
-        if (P.ml.simplified) {
+        if constexpr (SIMP) {
           put(V_YP, y);
           put(V_YGP, yg);
           dtp = dt;
@@ -808,7 +812,7 @@ struct Solver {
 };
 
 // One warp per sample, persistent work queue (same outer protocol as the plain kernel).
-template <int MC, int RPT>
+template <int MC, int RPT, bool SIMP>
 __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_constant__ AdvanceParams P) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
@@ -819,7 +823,7 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
     return;
   }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  Solver<MC, RPT> S{P, tables, tables + L.blob_bytes + warp * P.ml.warp_bytes, lane};
+  Solver<MC, RPT, SIMP> S{P, tables, tables + L.blob_bytes + warp * P.ml.warp_bytes, lane};
   const int m = L.m;
   const int n_items = P.n_items_dev ? *P.n_items_dev : P.n_items;
   int* stats = S.template w<int>(P.ml.stats);
@@ -870,7 +874,7 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
       S.template w<double>(P.ml.q)[L.R] = 0.0;
       S.template w<float>(P.ml.d32)[L.NF] = 0.f;
     }
-    if (P.ml.simplified)
+    if constexpr (SIMP)
       for (int j = lane; j < MC; j += 32) S.template w<float>(P.ml.ybuf)[j] = 0.f;  // leading zeros of apply_inverse
     S.have_inv = false;
     __syncwarp();

@@ -1,17 +1,19 @@
-// Instantiation of the mixed-precision kernel for MC=24 columns and 1 row(s) per lane (one
-// translation unit per shape so the shapes compile in parallel).
+// Instantiation of the FP32-LU mixed-precision kernel for MC=24 columns and 1 row(s) per
+// lane (one translation unit per kernel so the kernels compile in parallel).
 #include "kernels_mixed_impl.cuh"
 
 namespace tchem_gb {
 
 cudaError_t launch_mixed_24_1(const AdvanceParams& P, int grid, int threads, size_t smem, cudaStream_t stream) {
-  auto k = mixed::trbdf2_mixed_kernel<24, 1>;
+  auto k = mixed::trbdf2_mixed_kernel<24, 1, false>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   k<<<grid, threads, smem, stream>>>(P);
   return cudaGetLastError();
 }
 
-const void* kernel_mixed_24_1() { return reinterpret_cast<const void*>(mixed::trbdf2_mixed_kernel<24, 1>); }
+const void* kernel_mixed_24_1() {
+  return reinterpret_cast<const void*>(mixed::trbdf2_mixed_kernel<24, 1, false>);
+}
 
 }  // namespace tchem_gb

@@ -1,0 +1,19 @@
+// Instantiation of the simplified-Newton (Gauss-Jordan inverse) mixed-precision kernel for MC=32 columns and 1 row(s) per
+// lane (one translation unit per kernel so the kernels compile in parallel).
+#include "kernels_mixed_impl.cuh"
+
+namespace tchem_gb {
+
+cudaError_t launch_simpl_32_1(const AdvanceParams& P, int grid, int threads, size_t smem, cudaStream_t stream) {
+  auto k = mixed::trbdf2_mixed_kernel<32, 1, true>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  k<<<grid, threads, smem, stream>>>(P);
+  return cudaGetLastError();
+}
+
+const void* kernel_simpl_32_1() {
+  return reinterpret_cast<const void*>(mixed::trbdf2_mixed_kernel<32, 1, true>);
+}
+
+}  // namespace tchem_gb
