@@ -132,11 +132,13 @@ int tchem_gb_scenario_read(const char* yaml_path, const tchem_gb_mech* mech, dou
 enum tchem_gb_form {
   TCHEM_GB_FORM_PLAIN_FP64 = 0, /* FP64 Newton LU: the parity form */
   TCHEM_GB_FORM_MIXED = 1,      /* FP32 Newton LU and solves, FP64 residual/state/error control */
-  /* Simplified Newton with an FP32 Gauss-Jordan inverse of I - c J: the inverse is formed at the
-     start of a step (or carried from the previous step's error filter when c changed by at most
-     30%) and reused by every Newton iteration of both stages; it is refreshed once per stage when
-     the iteration contracts slower than 0.5. Newton stops when every component of the FP64
-     correction is below tol_newton (abs + rel |y_i|) and the reference's 2-norm test holds. The
+  /* Simplified Newton with an FP32 Gauss-Jordan inverse of I - c J: the inverse is carried from
+     the previous step's error filter while c changed by at most 30% (else formed at the first
+     iterate) and reused by every Newton iteration of both stages; it is re-formed once per stage
+     when the correction shrinks by less than half. Newton stops when every component of the FP64
+     correction satisfies |dx_i| <= atol/sqrt(m) + rtol |y_i| (tol_newton), which implies the
+     reference's 2-norm test. Stage guesses: the quadratic through the last step's y_n,
+     y_{n+gamma}, y_{n+1} (stage 1) and the quadratic through y_n, f_n, y_{n+gamma} (stage 2). The
      local-error filter uses a fresh inverse of I - c J(y_{n+1}), the matrix of the reference's
      last Newton iteration, so the step-size sequence follows the FP64 form. jacobian_interval is
      not used. */

@@ -1,0 +1,106 @@
+// C++ face of the engine with the reference's names and argument order
+// (TChem::AtmosphericChemistry, src/core/TChem_AtmosphericChemistry.hpp:47-157), over raw device
+// pointers instead of Kokkos views. Header-only; link against libtchem_gb.so.
+//
+//   TChem::AtmosphericChemistry::runDeviceBatch(policy, tol_newton, tol_time, fac, tadv, state,
+//                                               t_out, dt_out, state_out, kmcd)
+// becomes
+//   tchem_gb::AtmosphericChemistry::runDeviceBatch(stream, tol_newton, tol_time, fac, tadv, state,
+//                                                  t_out, dt_out, state_out, kmcd, nbatch)
+//
+// Errors throw std::logic_error, as TCHEM_CHECK_ERROR does in the reference
+// (src/core/TChem_Util.hpp:108-114); per-sample failures keep the reference convention
+// (dt_out < 0, state_out = 0, t_out = t_end) and are detailed in the optional status array.
+#pragma once
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "tchem_gb.h"
+
+namespace tchem_gb {
+
+inline void check(int rc, const char* where) {
+  if (rc != TCHEM_GB_OK) throw std::logic_error(std::string(where) + ": " + tchem_gb_last_error());
+}
+
+// Owning handle of a parsed mechanism (KineticModelData + KineticModelNCAR_ConstData).
+class KineticModel {
+ public:
+  explicit KineticModel(const std::string& yaml_path, const char* echo_path = nullptr) {
+    check(tchem_gb_mech_create_from_file(yaml_path.c_str(), echo_path, &m_), "tchem_gb_mech_create_from_file");
+  }
+  ~KineticModel() { tchem_gb_mech_destroy(m_); }
+  KineticModel(const KineticModel&) = delete;
+  KineticModel& operator=(const KineticModel&) = delete;
+  const tchem_gb_mech* handle() const { return m_; }
+  tchem_gb_kmcd_view view() const {
+    tchem_gb_kmcd_view v{};
+    check(tchem_gb_mech_host_view(m_, &v), "tchem_gb_mech_host_view");
+    return v;
+  }
+
+ private:
+  tchem_gb_mech* m_ = nullptr;
+};
+
+struct AtmosphericChemistry {
+  // getWorkSpaceSize(kmcd) for a batch of nbatch samples, in bytes of device memory.
+  static size_t getWorkSpaceSize(const KineticModel& kmcd, int nbatch, int form = TCHEM_GB_FORM_PLAIN_FP64) {
+    const tchem_gb_mech* h = kmcd.handle();
+    tchem_gb_advance_opts o{};
+    o.form = form;
+    const size_t n = tchem_gb_workspace_bytes(&h, 1, nbatch, &o);
+    if (n == 0) check(TCHEM_GB_ERR_ARG, "tchem_gb_workspace_bytes");
+    return n;
+  }
+
+  // runDeviceBatch with one mechanism for every sample. All arrays are device pointers with the
+  // reference's shapes: tol_newton[2], tol_time[m][2], tadv[nbatch], state[nbatch][nSpec+3],
+  // t_out/dt_out[nbatch], state_out[nbatch][nSpec+3] (may equal state). fac is accepted and
+  // ignored (the Jacobian is analytic).
+  static void runDeviceBatch(void* stream, const double* tol_newton, const double* tol_time, const double* fac,
+                             const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
+                             double* state_out, const KineticModel& kmcd, int nbatch, int32_t* status,
+                             int form = TCHEM_GB_FORM_PLAIN_FP64, void* workspace = nullptr,
+                             size_t workspace_bytes = 0) {
+    const tchem_gb_mech* h = kmcd.handle();
+    tchem_gb_advance_opts o{};
+    o.form = form;
+    check(tchem_gb_time_advance(&h, 1, nullptr, nbatch, tol_newton, tol_time, fac, tadv, state, t_out, dt_out,
+                                state_out, status, nullptr, workspace, workspace_bytes, &o, stream),
+          "tchem_gb_time_advance");
+  }
+
+  // The per-sample-mechanism overload (kmcds[B] in the reference): mech_of_sample[nbatch] is a
+  // device array of indices into kmcds.
+  static void runDeviceBatch(void* stream, const double* tol_newton, const double* tol_time, const double* fac,
+                             const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
+                             double* state_out, const std::vector<const KineticModel*>& kmcds,
+                             const int32_t* mech_of_sample, int nbatch, int32_t* status,
+                             int form = TCHEM_GB_FORM_PLAIN_FP64) {
+    std::vector<const tchem_gb_mech*> hs;
+    for (const KineticModel* k : kmcds) hs.push_back(k->handle());
+    tchem_gb_advance_opts o{};
+    o.form = form;
+    check(tchem_gb_time_advance(hs.data(), static_cast<int>(hs.size()), mech_of_sample, nbatch, tol_newton, tol_time,
+                                fac, tadv, state, t_out, dt_out, state_out, status, nullptr, nullptr, 0, &o, stream),
+          "tchem_gb_time_advance");
+  }
+
+  // runHostBatch: host arrays, synchronous.
+  static void runHostBatch(const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
+                           const double* state, double* t_out, double* dt_out, double* state_out,
+                           const KineticModel& kmcd, int nbatch, int32_t* status,
+                           int form = TCHEM_GB_FORM_PLAIN_FP64) {
+    const tchem_gb_mech* h = kmcd.handle();
+    tchem_gb_advance_opts o{};
+    o.form = form;
+    check(tchem_gb_time_advance_hostbuf(&h, 1, nullptr, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out,
+                                        state_out, status, nullptr, &o, nullptr),
+          "tchem_gb_time_advance_hostbuf");
+  }
+};
+
+}  // namespace tchem_gb

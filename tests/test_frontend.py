@@ -165,3 +165,31 @@ def test_library_exports_every_declared_symbol():
     lib = C.CDLL(str(_capi.LIB_PATH))
     missing = [n for n in sorted(names) if not hasattr(lib, n)]
     assert not missing, missing
+
+
+def test_cpp_shim_compiles_links_and_parses(tmp_path):
+    """The C++ face in include/tchem_gb_atm.hpp builds against the library and parses a mechanism
+    with the reference's names (host-only calls, no GPU)."""
+    import shutil
+    import subprocess
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    src = tmp_path / "shim.cpp"
+    src.write_text(
+        '#include "tchem_gb_atm.hpp"\n#include <cstdio>\n'
+        "int main(int argc, char** argv) {\n"
+        "  tchem_gb::KineticModel km(argv[1]);\n"
+        "  tchem_gb_kmcd_view v = km.view();\n"
+        '  std::printf("%d %d %d\\n", v.nSpec, v.nConstSpec, v.nReac);\n'
+        "  try { tchem_gb::KineticModel bad(\"/nonexistent.yaml\"); } catch (const std::logic_error&) { return 0; }\n"
+        "  return 1;\n}\n")
+    exe = tmp_path / "shim"
+    libdir = Path(_capi.LIB_PATH).parent
+    r = subprocess.run([cxx, "-std=c++17", f"-I{ROOT / 'include'}", str(src), "-o", str(exe), f"-L{libdir}",
+                        "-ltchem_gb", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe), str(mech_path("cb05cl_ae5.yaml"))], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    km = KineticModel.from_file(mech_path("cb05cl_ae5.yaml"))
+    assert out.stdout.split() == [str(km.nSpec), str(km.nConstSpec), str(km.nReac)]
