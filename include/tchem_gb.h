@@ -58,7 +58,8 @@ enum tchem_gb_sample_status {
   TCHEM_GB_SAMPLE_NEGATIVE_DT = 3, /* dt_in < 0: returned without touching the outputs */
   TCHEM_GB_SAMPLE_NONFINITE = 4,   /* non-finite value in the state or a step */
   TCHEM_GB_SAMPLE_DT_UNDERFLOW = 5, /* step size reached 0 before t_end */
-  TCHEM_GB_SAMPLE_BAD_MECH = 6      /* mech_of_sample names no mechanism of the call */
+  TCHEM_GB_SAMPLE_BAD_MECH = 6,     /* mech_of_sample names no mechanism of the call */
+  TCHEM_GB_SAMPLE_TAPE_FULL = 7     /* more accepted steps than the trajectory record holds */
 };
 
 /* Mirrors TChem::TimeAdvance (src/core/TChem_Util.hpp:469-477), same field order and types. */
@@ -182,6 +183,36 @@ int tchem_gb_time_advance_hostbuf(const tchem_gb_mech* const* mechs, int n_mechs
                                   const tchem_gb_tadv* tadv, const double* state, double* t_out,
                                   double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats,
                                   const tchem_gb_advance_opts* opts, void* stream);
+
+/* ---- Discrete adjoint (plain FP64 form, one mechanism) ------------------------------------
+ * No counterpart in the reference (its TR-BDF2 has no adjoint); these extend runDeviceBatch
+ * (src/core/TChem_AtmosphericChemistry.hpp:83-105) with the trajectory record and the
+ * vector-Jacobian product of the end state.
+ *
+ * tchem_gb_time_advance_record: tchem_gb_time_advance in the plain FP64 form, one mechanism,
+ * that also records per sample the accepted step sizes tape_dt[nbatch][tape_cap], the state of
+ * the active species at the start of steps 0, 32, 64, ... in
+ * tape_ckpt[nbatch][tape_cap/32 + 1][m], and the step count tape_nsteps[nbatch]. A sample that
+ * needs more than tape_cap steps ends with status TCHEM_GB_SAMPLE_TAPE_FULL. k_scale[nReac]
+ * (device, optional) multiplies each reaction's rate constant (exp(theta_r)). */
+int tchem_gb_time_advance_record(const tchem_gb_mech* mech, int nbatch, const double* tol_newton,
+                                 const double* tol_time, const double* k_scale, const tchem_gb_tadv* tadv,
+                                 const double* state, double* t_out, double* dt_out, double* state_out,
+                                 int32_t* status, tchem_gb_sample_stats* stats, double* tape_dt, double* tape_ckpt,
+                                 int32_t* tape_nsteps, int tape_cap, void* stream);
+
+/* Device workspace (bytes) of tchem_gb_adjoint for nbatch samples. */
+size_t tchem_gb_adjoint_workspace_bytes(const tchem_gb_mech* mech, int nbatch);
+
+/* Discrete adjoint of a recorded run: given lambda[nbatch][m] = dL/dy(t_end) for the active
+ * species, writes grad_x0[nbatch][m] = dL/dy(t_0) and grad_k[nbatch][nReac] = dL/dtheta_r, where
+ * exp(theta_r) multiplies reaction r's rate constant (so theta_r is the log of its
+ * pre-exponential factors). The step sequence is the recorded one; state, tadv, tol_newton and
+ * k_scale must be those of the recording call. status[nbatch] as for the time advance. */
+int tchem_gb_adjoint(const tchem_gb_mech* mech, int nbatch, const double* tol_newton, const double* k_scale,
+                     const tchem_gb_tadv* tadv, const double* state, const double* tape_dt, const double* tape_ckpt,
+                     const int32_t* tape_nsteps, int tape_cap, const double* lambda, double* grad_x0, double* grad_k,
+                     int32_t* status, void* workspace, size_t workspace_bytes, void* stream);
 
 /* Synchronizes `stream`, then reads and clears the device error word of `workspace` (NULL: the
  * library-owned workspace). *device_error is 0 when no kernel reported a timed-out wait. */

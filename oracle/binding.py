@@ -27,6 +27,15 @@ def load() -> C.CDLL:
         L.oracle_time_advance.restype = C.c_int
         L.oracle_time_advance.argtypes = [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                           C.c_int, C.c_int, C.c_int]
+        i = C.c_int
+        L.oracle_time_advance_record.restype = i
+        L.oracle_time_advance_record.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i, i]
+        L.oracle_replay.restype = i
+        L.oracle_replay.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, i, vp, i]
+        L.oracle_adjoint.restype = i
+        L.oracle_adjoint.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, i]
+        L.oracle_tangent.restype = i
+        L.oracle_tangent.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, i]
         _lib = L
     return _lib
 
@@ -95,6 +104,75 @@ class Oracle:
         if rc != 0:
             raise RuntimeError(f"oracle_time_advance returned {rc}")
         return state_out, t_out, dt_out, status, stats
+
+
+class Tape:
+    """Recorded accepted step sizes of a forward run (for replay, adjoint and tangent)."""
+
+    def __init__(self, dt: np.ndarray, nsteps: np.ndarray):
+        self.dt, self.nsteps = dt, nsteps
+
+    @property
+    def cap(self) -> int:
+        return self.dt.shape[1]
+
+
+def _a(x, dtype=np.float64):
+    return np.ascontiguousarray(x, dtype=dtype)
+
+
+def record(o: "Oracle", tadv, state, tol_newton, tol_time, cap: int, k_scale=None, nthreads: int = 0):
+    """FP64 forward run recording the step sequence: (state_out, t_out, dt_out, status, Tape)."""
+    B = state.shape[0]
+    state = _a(state)
+    out = state.copy()
+    t_out, dt_out = np.zeros(B), np.zeros(B)
+    status = np.zeros(B, dtype=np.int32)
+    dt = np.zeros((B, cap))
+    ns = np.zeros(B, dtype=np.int32)
+    rc = o.lib.oracle_time_advance_record(o._vp(0), B, _p(_a(tol_newton)), _p(_a(tol_time)),
+                                          _p(None if k_scale is None else _a(k_scale)), _p(np.ascontiguousarray(tadv)),
+                                          _p(state), _p(t_out), _p(dt_out), _p(out), _p(status), _p(dt), _p(ns), cap,
+                                          nthreads)
+    assert rc == 0, rc
+    return out, t_out, dt_out, status, Tape(dt, ns)
+
+
+def replay(o: "Oracle", tadv, state, tol_newton, tape: Tape, k_scale=None, nthreads: int = 0) -> np.ndarray:
+    """End states [B][m] of the recorded steps re-run from state (fixed step sequence)."""
+    B = state.shape[0]
+    m = o.models[0].nSpec - o.models[0].nConstSpec
+    y = np.zeros((B, m))
+    rc = o.lib.oracle_replay(o._vp(0), B, _p(_a(tol_newton)), _p(None if k_scale is None else _a(k_scale)),
+                             _p(np.ascontiguousarray(tadv)), _p(_a(state)), _p(tape.dt), _p(tape.nsteps), tape.cap,
+                             _p(y), nthreads)
+    assert rc == 0, rc
+    return y
+
+
+def adjoint(o: "Oracle", tadv, state, tol_newton, tape: Tape, lam, k_scale=None, nthreads: int = 0):
+    """(dL/dy0 [B][m], dL/dtheta [B][R]) for the cotangent lam = dL/dy_end [B][m]."""
+    B = state.shape[0]
+    km = o.models[0]
+    m, R = km.nSpec - km.nConstSpec, km.nReac
+    gx, gk = np.zeros((B, m)), np.zeros((B, R))
+    rc = o.lib.oracle_adjoint(o._vp(0), B, _p(_a(tol_newton)), _p(None if k_scale is None else _a(k_scale)),
+                              _p(np.ascontiguousarray(tadv)), _p(_a(state)), _p(tape.dt), _p(tape.nsteps), tape.cap,
+                              _p(_a(lam)), _p(gx), _p(gk), nthreads)
+    assert rc == 0, rc
+    return gx, gk
+
+
+def tangent(o: "Oracle", tadv, state, tol_newton, tape: Tape, dx0, dtheta, k_scale=None, nthreads: int = 0):
+    """Forward sensitivities dy_end [B][m] along (dx0 [B][m], dtheta [B][R])."""
+    B = state.shape[0]
+    m = o.models[0].nSpec - o.models[0].nConstSpec
+    dy = np.zeros((B, m))
+    rc = o.lib.oracle_tangent(o._vp(0), B, _p(_a(tol_newton)), _p(None if k_scale is None else _a(k_scale)),
+                              _p(np.ascontiguousarray(tadv)), _p(_a(state)), _p(tape.dt), _p(tape.nsteps), tape.cap,
+                              _p(_a(dx0)), _p(_a(dtheta)), _p(dy), nthreads)
+    assert rc == 0, rc
+    return dy
 
 
 def library_path() -> Path:

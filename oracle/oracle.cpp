@@ -152,6 +152,19 @@ struct DenseLU {
     }
     return true;
   }
+  // x = A^{-T} b with the same factors: U^T z = b, L^T v = z, x = P^T v.
+  void solve_t(const double* b, double* x) {
+    for (int i = 0; i < n; ++i) w[i] = static_cast<T>(b[i]);
+    for (int j = 0; j < n; ++j) {
+      w[j] /= a[static_cast<size_t>(j) * n + j];
+      for (int l = j + 1; l < n; ++l) w[l] -= a[static_cast<size_t>(j) * n + l] * w[j];
+    }
+    for (int k = n - 1; k > 0; --k)
+      for (int i = 0; i < k; ++i) w[i] -= a[static_cast<size_t>(k) * n + i] * w[k];
+    for (int k = n - 1; k >= 0; --k)
+      if (piv[k] != k) std::swap(w[k], w[piv[k]]);
+    for (int i = 0; i < n; ++i) x[i] = static_cast<double>(w[i]);
+  }
   // x = A^{-1} b (b and x in double, arithmetic in T).
   void solve(const double* b, double* x) {
     for (int i = 0; i < n; ++i) w[i] = static_cast<T>(b[i]);
@@ -189,7 +202,11 @@ struct Sample {
   bool have_lu = false, fresh = false;
   double c_lu = 0.0;
 
-  Sample(const tchem_gb_kmcd_view& km_, double T, double p, const double* xconst)
+  // trajectory record (adjoint): accepted step sizes, or null
+  double* tape_dt = nullptr;
+  int tape_cap = 0;
+
+  Sample(const tchem_gb_kmcd_view& km_, double T, double p, const double* xconst, const double* k_scale = nullptr)
       : km(km_), m(km_.nSpec - km_.nConstSpec), n(km_.nSpec) {
     kfor.assign(km.nReac, 0.0);
     rop.assign(km.nReac, 0.0);
@@ -197,6 +214,8 @@ struct Sample {
     J.assign(static_cast<size_t>(m) * m, 0.0);
     for (int i = 0; i < n - m; ++i) concX[m + i] = xconst[i];
     kforward(km, T, p, kfor.data());
+    if (k_scale)
+      for (int r = 0; r < km.nReac; ++r) kfor[r] *= k_scale[r];
     lu.resize(m);
   }
   void f(const double* y, double* out) {
@@ -372,6 +391,10 @@ struct Sample {
       }
       if (!std::isfinite(err)) { status = TCHEM_GB_SAMPLE_NONFINITE; break; }
       if (err <= 1.0 || dt <= dt_min) {
+        if (tape_dt) {
+          if (st.n_steps >= tape_cap) { status = TCHEM_GB_SAMPLE_TAPE_FULL; break; }
+          tape_dt[st.n_steps] = dt;
+        }
         t = last ? t_end : t + dt;
         if (s.simplified) {
           std::copy(y, y + m, yp.begin());
@@ -441,6 +464,156 @@ void run_batch(const tchem_gb_kmcd_view* const* kms, const int32_t* mech_of_samp
   }
 }
 
+// --- discrete adjoint and forward sensitivities of the plain form ------------------------------
+// On a recorded step sequence (the step-size control is not differentiated). Stages per step, with
+// c = gamma/2 dt: (1) y_g - c f(y_g) = y_n + c f(y_n); (2) y_1 - c f(y_1) = cg y_g - cn y_n.
+
+// nu_r . mu over the active species of reaction r.
+double nu_dot(const tchem_gb_kmcd_view& km, int r, const double* mu) {
+  const int m = km.nSpec - km.nConstSpec, S = km.maxSpecInReac, joff = S / 2;
+  double d = 0.0;
+  for (int j = 0; j < km.reacNreac[r]; ++j) {
+    const int k = km.reacSidx[r * S + j];
+    if (k < m) d += km.reacNuki[r * S + j] * mu[k];
+  }
+  for (int j = 0; j < km.reacNprod[r]; ++j) {
+    const int k = km.reacSidx[r * S + j + joff];
+    if (k < m) d += km.reacNuki[r * S + j + joff] * mu[k];
+  }
+  return d;
+}
+
+// out += scale * sum_r nu_r q_r dtheta_r (the rates of progress q from the last f()).
+void add_ftheta(const tchem_gb_kmcd_view& km, const double* rop, const double* dth, double scale, double* out) {
+  const int m = km.nSpec - km.nConstSpec, S = km.maxSpecInReac, joff = S / 2;
+  for (int r = 0; r < km.nReac; ++r) {
+    const double q = scale * rop[r] * dth[r];
+    for (int j = 0; j < km.reacNreac[r]; ++j) {
+      const int k = km.reacSidx[r * S + j];
+      if (k < m) out[k] += km.reacNuki[r * S + j] * q;
+    }
+    for (int j = 0; j < km.reacNprod[r]; ++j) {
+      const int k = km.reacSidx[r * S + j + joff];
+      if (k < m) out[k] += km.reacNuki[r * S + j + joff] * q;
+    }
+  }
+}
+
+// Replays the recorded steps from y0: yn[j], yg[j] (m each) per step and the end state.
+bool replay(Sample<double>& S, const double* y0, const double* dts, int nsteps, const Settings& s,
+            std::vector<double>& yn, std::vector<double>& yg, std::vector<double>& yend) {
+  const int m = S.m;
+  const double gamma = 2.0 - std::sqrt(2.0), d = 0.5 * gamma;
+  const double cg = 1.0 / (gamma * (2.0 - gamma)), cn = (1.0 - gamma) * (1.0 - gamma) / (gamma * (2.0 - gamma));
+  std::vector<double> y(y0, y0 + m), fn(m), rv(m), g1(m), fy(m), g(m), dx(m);
+  yn.assign(static_cast<size_t>(nsteps) * m, 0.0);
+  yg.assign(static_cast<size_t>(nsteps) * m, 0.0);
+  S.f(y.data(), fn.data());
+  for (int j = 0; j < nsteps; ++j) {
+    const double c = d * dts[j];
+    std::copy(y.begin(), y.end(), yn.begin() + static_cast<size_t>(j) * m);
+    for (int i = 0; i < m; ++i) { rv[i] = y[i] + c * fn[i]; g1[i] = y[i]; }
+    if (!S.newton(g1.data(), rv.data(), c, s, fy, g, dx)) return false;
+    std::copy(g1.begin(), g1.end(), yg.begin() + static_cast<size_t>(j) * m);
+    for (int i = 0; i < m; ++i) { rv[i] = cg * g1[i] - cn * y[i]; y[i] = g1[i]; }
+    if (!S.newton(y.data(), rv.data(), c, s, fy, g, dx)) return false;
+    S.f(y.data(), fn.data());
+  }
+  yend = y;
+  return true;
+}
+
+// lambda (in: dL/dy_end, out: dL/dy0) and gk += dL/dtheta over the recorded steps.
+bool adjoint_sweep(Sample<double>& S, const std::vector<double>& yn, const std::vector<double>& yg,
+                   const std::vector<double>& yend, const double* dts, int nsteps, double* lam, double* gk) {
+  const int m = S.m, R = S.km.nReac;
+  const double gamma = 2.0 - std::sqrt(2.0), d = 0.5 * gamma;
+  const double cg = 1.0 / (gamma * (2.0 - gamma)), cn = (1.0 - gamma) * (1.0 - gamma) / (gamma * (2.0 - gamma));
+  std::vector<double> mu1(m), mu2(m), tmp(m), y1(yend);
+  for (int j = nsteps - 1; j >= 0; --j) {
+    const double c = d * dts[j];
+    const double* ynj = yn.data() + static_cast<size_t>(j) * m;
+    const double* ygj = yg.data() + static_cast<size_t>(j) * m;
+    S.jac(y1.data());
+    if (!S.lu.factor(S.J.data(), c)) return false;
+    S.lu.solve_t(lam, mu2.data());
+    S.f(y1.data(), tmp.data());
+    for (int r = 0; r < R; ++r) gk[r] += c * S.rop[r] * nu_dot(S.km, r, mu2.data());
+    for (int i = 0; i < m; ++i) tmp[i] = cg * mu2[i];
+    S.jac(ygj);
+    if (!S.lu.factor(S.J.data(), c)) return false;
+    S.lu.solve_t(tmp.data(), mu1.data());
+    S.f(ygj, tmp.data());
+    for (int r = 0; r < R; ++r) gk[r] += c * S.rop[r] * nu_dot(S.km, r, mu1.data());
+    S.f(ynj, tmp.data());
+    for (int r = 0; r < R; ++r) gk[r] += c * S.rop[r] * nu_dot(S.km, r, mu1.data());
+    S.jac(ynj);
+    for (int jj = 0; jj < m; ++jj) {
+      double acc = 0.0;
+      for (int i = 0; i < m; ++i) acc += S.J[static_cast<size_t>(i) * m + jj] * mu1[i];
+      lam[jj] = -cn * mu2[jj] + mu1[jj] + c * acc;
+    }
+    std::copy(ynj, ynj + m, y1.begin());
+  }
+  return true;
+}
+
+// Forward sensitivity: s (in: dy0, out: dy_end) along dtheta over the recorded steps.
+bool tangent_sweep(Sample<double>& S, const std::vector<double>& yn, const std::vector<double>& yg,
+                   const std::vector<double>& yend, const double* dts, int nsteps, const double* dth, double* sv) {
+  const int m = S.m;
+  const double gamma = 2.0 - std::sqrt(2.0), d = 0.5 * gamma;
+  const double cg = 1.0 / (gamma * (2.0 - gamma)), cn = (1.0 - gamma) * (1.0 - gamma) / (gamma * (2.0 - gamma));
+  std::vector<double> b(m), sg(m), tmp(m);
+  for (int j = 0; j < nsteps; ++j) {
+    const double c = d * dts[j];
+    const double* ynj = yn.data() + static_cast<size_t>(j) * m;
+    const double* ygj = yg.data() + static_cast<size_t>(j) * m;
+    const double* y1 = j + 1 < nsteps ? yn.data() + static_cast<size_t>(j + 1) * m : yend.data();
+    S.jac(ynj);
+    for (int i = 0; i < m; ++i) {
+      double acc = 0.0;
+      for (int k = 0; k < m; ++k) acc += S.J[static_cast<size_t>(i) * m + k] * sv[k];
+      b[i] = sv[i] + c * acc;
+    }
+    S.f(ynj, tmp.data());
+    add_ftheta(S.km, S.rop.data(), dth, c, b.data());
+    S.f(ygj, tmp.data());
+    add_ftheta(S.km, S.rop.data(), dth, c, b.data());
+    S.jac(ygj);
+    if (!S.lu.factor(S.J.data(), c)) return false;
+    S.lu.solve(b.data(), sg.data());
+    for (int i = 0; i < m; ++i) b[i] = cg * sg[i] - cn * sv[i];
+    S.f(y1, tmp.data());
+    add_ftheta(S.km, S.rop.data(), dth, c, b.data());
+    S.jac(y1);
+    if (!S.lu.factor(S.J.data(), c)) return false;
+    S.lu.solve(b.data(), sv);
+  }
+  return true;
+}
+
+struct SampleSetup {
+  std::vector<double> y0, xconst;
+  double T = 0.0, p = 0.0;
+};
+
+SampleSetup setup_row(const tchem_gb_kmcd_view& km, const double* state, int b) {
+  const int n = km.nSpec, m = n - km.nConstSpec;
+  const double* row = state + static_cast<size_t>(b) * (n + 3);
+  SampleSetup u;
+  u.p = row[1];
+  u.T = row[2];
+  u.y0.assign(row + 3, row + 3 + m);
+  u.xconst.assign(row + 3 + m, row + 3 + n);
+  return u;
+}
+
+Settings replay_settings(const tchem_gb_tadv& ta, const double* tol_newton) {
+  return Settings{ta.max_num_newton_iterations, std::max(1, ta.jacobian_interval), ta.num_time_iterations_per_interval,
+                  0, false, tol_newton[0], tol_newton[1], nullptr};
+}
+
 }  // namespace
 
 extern "C" {
@@ -494,6 +667,132 @@ int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const
   if (nthreads > 0) omp_set_num_threads(prev);
 #endif
   return TCHEM_GB_OK;
+}
+
+int oracle_time_advance_record(const tchem_gb_kmcd_view* km, int nbatch, const double* tol_newton,
+                               const double* tol_time, const double* k_scale, const tchem_gb_tadv* tadv,
+                               const double* state, double* t_out, double* dt_out, double* state_out,
+                               int32_t* status, double* tape_dt, int32_t* tape_nsteps, int tape_cap, int nthreads) {
+  if (!km || nbatch < 0 || !tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out || !state_out || !status ||
+      !tape_dt || !tape_nsteps || tape_cap < 1)
+    return TCHEM_GB_ERR_ARG;
+  const int n = km->nSpec, m = n - km->nConstSpec;
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int b = 0; b < nbatch; ++b) {
+    const tchem_gb_tadv& ta = tadv[b];
+    const SampleSetup u = setup_row(*km, state, b);
+    Sample<double> smp(*km, u.T, u.p, u.xconst.data(), k_scale);
+    smp.tape_dt = tape_dt + static_cast<size_t>(b) * tape_cap;
+    smp.tape_cap = tape_cap;
+    Settings s{ta.max_num_newton_iterations, std::max(1, ta.jacobian_interval), ta.num_time_iterations_per_interval,
+               0, false, tol_newton[0], tol_newton[1], tol_time};
+    std::vector<double> y(u.y0);
+    double to = 0.0, dto = 0.0;
+    status[b] = smp.integrate(y.data(), ta.tbeg, ta.tend, ta.dt, ta.dtmin, ta.dtmax, s, to, dto);
+    tape_nsteps[b] = smp.st.n_steps;
+    double* out = state_out + static_cast<size_t>(b) * (n + 3);
+    const double* row = state + static_cast<size_t>(b) * (n + 3);
+    std::copy(row, row + n + 3, out);
+    for (int i = 0; i < m; ++i) out[3 + i] = y[i];
+    t_out[b] = to;
+    dt_out[b] = dto;
+  }
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(prev);
+#endif
+  return TCHEM_GB_OK;
+}
+
+int oracle_replay(const tchem_gb_kmcd_view* km, int nbatch, const double* tol_newton, const double* k_scale,
+                  const tchem_gb_tadv* tadv, const double* state, const double* tape_dt, const int32_t* tape_nsteps,
+                  int tape_cap, double* y_end, int nthreads) {
+  if (!km || nbatch < 0 || !tol_newton || !tadv || !state || !tape_dt || !tape_nsteps || !y_end) return TCHEM_GB_ERR_ARG;
+  const int m = km->nSpec - km->nConstSpec;
+  int rc = TCHEM_GB_OK;
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int b = 0; b < nbatch; ++b) {
+    const SampleSetup u = setup_row(*km, state, b);
+    Sample<double> smp(*km, u.T, u.p, u.xconst.data(), k_scale);
+    std::vector<double> yn, yg, ye;
+    if (!replay(smp, u.y0.data(), tape_dt + static_cast<size_t>(b) * tape_cap, tape_nsteps[b],
+                replay_settings(tadv[b], tol_newton), yn, yg, ye))
+      rc = TCHEM_GB_ERR_DEVICE;
+    else
+      std::copy(ye.begin(), ye.end(), y_end + static_cast<size_t>(b) * m);
+  }
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(prev);
+#endif
+  return rc;
+}
+
+int oracle_adjoint(const tchem_gb_kmcd_view* km, int nbatch, const double* tol_newton, const double* k_scale,
+                   const tchem_gb_tadv* tadv, const double* state, const double* tape_dt, const int32_t* tape_nsteps,
+                   int tape_cap, const double* lambda, double* grad_x0, double* grad_k, int nthreads) {
+  if (!km || nbatch < 0 || !tol_newton || !tadv || !state || !tape_dt || !tape_nsteps || !lambda || !grad_x0 ||
+      !grad_k)
+    return TCHEM_GB_ERR_ARG;
+  const int m = km->nSpec - km->nConstSpec, R = km->nReac;
+  int rc = TCHEM_GB_OK;
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int b = 0; b < nbatch; ++b) {
+    const SampleSetup u = setup_row(*km, state, b);
+    Sample<double> smp(*km, u.T, u.p, u.xconst.data(), k_scale);
+    std::vector<double> yn, yg, ye;
+    const double* dts = tape_dt + static_cast<size_t>(b) * tape_cap;
+    double* lam = grad_x0 + static_cast<size_t>(b) * m;
+    double* gk = grad_k + static_cast<size_t>(b) * R;
+    std::copy(lambda + static_cast<size_t>(b) * m, lambda + static_cast<size_t>(b + 1) * m, lam);
+    std::fill(gk, gk + R, 0.0);
+    if (!replay(smp, u.y0.data(), dts, tape_nsteps[b], replay_settings(tadv[b], tol_newton), yn, yg, ye) ||
+        !adjoint_sweep(smp, yn, yg, ye, dts, tape_nsteps[b], lam, gk))
+      rc = TCHEM_GB_ERR_DEVICE;
+  }
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(prev);
+#endif
+  return rc;
+}
+
+int oracle_tangent(const tchem_gb_kmcd_view* km, int nbatch, const double* tol_newton, const double* k_scale,
+                   const tchem_gb_tadv* tadv, const double* state, const double* tape_dt, const int32_t* tape_nsteps,
+                   int tape_cap, const double* dx0, const double* dtheta, double* dy_end, int nthreads) {
+  if (!km || nbatch < 0 || !tol_newton || !tadv || !state || !tape_dt || !tape_nsteps || !dx0 || !dtheta || !dy_end)
+    return TCHEM_GB_ERR_ARG;
+  const int m = km->nSpec - km->nConstSpec, R = km->nReac;
+  int rc = TCHEM_GB_OK;
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int b = 0; b < nbatch; ++b) {
+    const SampleSetup u = setup_row(*km, state, b);
+    Sample<double> smp(*km, u.T, u.p, u.xconst.data(), k_scale);
+    std::vector<double> yn, yg, ye;
+    const double* dts = tape_dt + static_cast<size_t>(b) * tape_cap;
+    double* sv = dy_end + static_cast<size_t>(b) * m;
+    std::copy(dx0 + static_cast<size_t>(b) * m, dx0 + static_cast<size_t>(b + 1) * m, sv);
+    if (!replay(smp, u.y0.data(), dts, tape_nsteps[b], replay_settings(tadv[b], tol_newton), yn, yg, ye) ||
+        !tangent_sweep(smp, yn, yg, ye, dts, tape_nsteps[b], dtheta + static_cast<size_t>(b) * R, sv))
+      rc = TCHEM_GB_ERR_DEVICE;
+  }
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(prev);
+#endif
+  return rc;
 }
 
 }  // extern "C"

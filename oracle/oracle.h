@@ -56,6 +56,29 @@ int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const
                         const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
                         tchem_gb_sample_stats* stats, int lu_fp32, int simplified, int nthreads);
 
+/* Discrete adjoint of the plain form on a recorded step sequence (the engine's
+ * tchem_gb_time_advance_record / tchem_gb_adjoint), restated densely on the CPU, one mechanism:
+ *   oracle_time_advance_record: oracle_time_advance (FP64) recording the accepted step sizes
+ *     tape_dt[nbatch][tape_cap] and counts tape_nsteps[nbatch]; k_scale[nReac] (optional)
+ *     multiplies every rate constant.
+ *   oracle_replay: the recorded steps re-run from state (no step-size control); y_end[nbatch][m].
+ *   oracle_adjoint: lambda[nbatch][m] = dL/dy_end -> grad_x0 = dL/dy0, grad_k[nbatch][nReac] =
+ *     dL/dtheta_r with k_r scaled by exp(theta_r).
+ *   oracle_tangent: forward sensitivities dy_end along (dx0[nbatch][m], dtheta[nbatch][nReac]). */
+int oracle_time_advance_record(const tchem_gb_kmcd_view* km, int nbatch, const double* tol_newton,
+                               const double* tol_time, const double* k_scale, const tchem_gb_tadv* tadv,
+                               const double* state, double* t_out, double* dt_out, double* state_out,
+                               int32_t* status, double* tape_dt, int32_t* tape_nsteps, int tape_cap, int nthreads);
+int oracle_replay(const tchem_gb_kmcd_view* km, int nbatch, const double* tol_newton, const double* k_scale,
+                  const tchem_gb_tadv* tadv, const double* state, const double* tape_dt, const int32_t* tape_nsteps,
+                  int tape_cap, double* y_end, int nthreads);
+int oracle_adjoint(const tchem_gb_kmcd_view* km, int nbatch, const double* tol_newton, const double* k_scale,
+                   const tchem_gb_tadv* tadv, const double* state, const double* tape_dt, const int32_t* tape_nsteps,
+                   int tape_cap, const double* lambda, double* grad_x0, double* grad_k, int nthreads);
+int oracle_tangent(const tchem_gb_kmcd_view* km, int nbatch, const double* tol_newton, const double* k_scale,
+                   const tchem_gb_tadv* tadv, const double* state, const double* tape_dt, const int32_t* tape_nsteps,
+                   int tape_cap, const double* dx0, const double* dtheta, double* dy_end, int nthreads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -10,6 +10,7 @@ namespace tchem_gb {
 
 constexpr int kMaxMechs = 64;       // mechanisms per time-advance call
 constexpr int kMaxGroupSlots = 8;   // structure-compatible mechanisms sharing one launch
+constexpr int kTapeSegment = 32;    // steps between trajectory checkpoints (adjoint)
 
 // Byte offsets of the sections of one warp's shared-memory region (mixed form). Kept in the
 // kernel parameters (constant bank) so section addresses cost no registers.
@@ -46,6 +47,13 @@ struct AdvanceParams {
   uint32_t warp_smem_bytes;
   int32_t* error_word;                          // device-side error report (bounded waits)
   MixedLayout ml;                               // mixed form only
+  // Trajectory record of the plain form for the discrete adjoint (tape_dt null: none): the
+  // accepted step sizes and the state at the start of every kTapeSegment-th step, per sample.
+  double* tape_dt;                              // [B][tape_cap]
+  double* tape_ckpt;                            // [B][tape_cap / kTapeSegment + 1][m]
+  int32_t* tape_nsteps;                         // [B]
+  int32_t tape_cap;
+  const double* k_scale;                        // [R] rate-constant multipliers (null: none)
 };
 
 }  // namespace tchem_gb

@@ -240,11 +240,25 @@ size_t tchem_gb_workspace_bytes(const tchem_gb_mech* const* mechs, int n_mechs, 
   }
 }
 
-int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
-                          const double* tol_newton, const double* tol_time, const double* /*fac*/,
-                          const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
-                          double* state_out, int32_t* status, tchem_gb_sample_stats* stats, void* workspace,
-                          size_t workspace_bytes, const tchem_gb_advance_opts* opts, void* stream_v) {
+}  // extern "C"
+
+namespace tchem_gb {
+namespace {
+
+// Trajectory-record arguments of the plain form (all null: no record).
+struct TapeArgs {
+  double* dt = nullptr;
+  double* ckpt = nullptr;
+  int32_t* nsteps = nullptr;
+  int cap = 0;
+  const double* k_scale = nullptr;
+};
+
+int time_advance_impl(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                      const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
+                      const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
+                      tchem_gb_sample_stats* stats, void* workspace, size_t workspace_bytes,
+                      const tchem_gb_advance_opts* opts, void* stream_v, const TapeArgs& tape) {
   if (!mechs || nbatch < 0) return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance: bad mechanisms or batch size");
   if (nbatch == 0) return TCHEM_GB_OK;  // empty arrays may come with null pointers
   if (!tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out || !state_out || !status)
@@ -328,12 +342,179 @@ int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const 
     P.warp_smem_bytes = gp.warp_smem;
     P.error_word = error_word;
     P.ml = gp.ml;
+    P.tape_dt = tape.dt;
+    P.tape_ckpt = tape.ckpt;
+    P.tape_nsteps = tape.nsteps;
+    P.tape_cap = tape.cap;
+    P.k_scale = tape.k_scale;
     if (gp.form == TCHEM_GB_FORM_MIXED || gp.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED)
       e = launch_trbdf2_mixed(P, gp.dev.L, gp.grid, gp.warps_per_block, gp.smem, gp.threads_per_sample, stream);
     else
       e = launch_trbdf2_fp64(P, gp.grid, gp.warps_per_block, gp.smem, stream);
     if (e != cudaSuccess) return cuda_fail(e, "time-advance kernel launch");
   }
+  return TCHEM_GB_OK;
+}
+
+}  // namespace
+}  // namespace tchem_gb
+
+extern "C" {
+
+int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
+                          const double* tol_newton, const double* tol_time, const double* /*fac*/,
+                          const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
+                          double* state_out, int32_t* status, tchem_gb_sample_stats* stats, void* workspace,
+                          size_t workspace_bytes, const tchem_gb_advance_opts* opts, void* stream_v) {
+  return time_advance_impl(mechs, n_mechs, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out,
+                           state_out, status, stats, workspace, workspace_bytes, opts, stream_v, TapeArgs{});
+}
+
+int tchem_gb_time_advance_record(const tchem_gb_mech* mech, int nbatch, const double* tol_newton,
+                                 const double* tol_time, const double* k_scale, const tchem_gb_tadv* tadv,
+                                 const double* state, double* t_out, double* dt_out, double* state_out,
+                                 int32_t* status, tchem_gb_sample_stats* stats, double* tape_dt, double* tape_ckpt,
+                                 int32_t* tape_nsteps, int tape_cap, void* stream) {
+  if (!mech) return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance_record: null mechanism");
+  if (nbatch > 0 && (!tape_dt || !tape_ckpt || !tape_nsteps || tape_cap < 1))
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance_record: null trajectory record or tape_cap < 1");
+  TapeArgs tape;
+  tape.dt = tape_dt;
+  tape.ckpt = tape_ckpt;
+  tape.nsteps = tape_nsteps;
+  tape.cap = tape_cap;
+  tape.k_scale = k_scale;
+  tchem_gb_advance_opts o{};
+  o.form = TCHEM_GB_FORM_PLAIN_FP64;
+  const tchem_gb_mech* mechs[1] = {mech};
+  return time_advance_impl(mechs, 1, nullptr, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out,
+                           status, stats, nullptr, 0, &o, stream, tape);
+}
+
+}  // extern "C"
+
+namespace tchem_gb {
+namespace {
+
+struct AdjointPlan {
+  int warps = 0, grid = 0, lda = 0;
+  bool matrix_in_smem = true;
+  size_t smem = 0, warp_smem = 0;
+  size_t seg_offset = 0, seg_stride = 0, gmat_offset = 0, gmat_stride = 0, bytes = 0;
+};
+
+AdjointPlan make_adjoint_plan(const MechLayout& L, int nbatch, int dev) {
+  const DeviceInfo info = device_info(dev);
+  AdjointPlan a;
+  a.lda = L.m | 1;
+  const size_t avail = static_cast<size_t>(info.max_smem_optin) - 16 - L.blob_bytes;
+  size_t ws = adjoint_warp_smem_bytes(L, a.lda, true);
+  if (ws > avail) {
+    a.matrix_in_smem = false;
+    ws = adjoint_warp_smem_bytes(L, a.lda, false);
+    if (ws > avail) throw std::invalid_argument("mechanism too large for the adjoint's shared-memory working set");
+  }
+  a.warps = static_cast<int>(std::min<size_t>(kMaxWarpsPerBlock, avail / ws));
+  a.warp_smem = ws;
+  a.smem = 16 + L.blob_bytes + a.warps * ws;
+  const void* k = adjoint_kernel_ptr(L.m);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(a.smem));
+  int bps = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k, a.warps * 32, a.smem) != cudaSuccess || bps < 1) bps = 1;
+  a.grid = std::max(1, std::min(info.sm_count * bps, (std::max(nbatch, 1) + a.warps - 1) / a.warps));
+  const size_t nw = static_cast<size_t>(a.grid) * a.warps;
+  size_t off = kHeaderBytes;
+  a.seg_stride = static_cast<size_t>(2 * kTapeSegment) * L.m;
+  a.seg_offset = off;
+  off += up256(sizeof(double) * a.seg_stride * nw);
+  if (!a.matrix_in_smem) {
+    a.gmat_stride = static_cast<size_t>(L.m) * a.lda;
+    a.gmat_offset = off;
+    off += up256(sizeof(double) * a.gmat_stride * nw);
+  }
+  a.bytes = off;
+  return a;
+}
+
+}  // namespace
+}  // namespace tchem_gb
+
+extern "C" {
+
+size_t tchem_gb_adjoint_workspace_bytes(const tchem_gb_mech* mech, int nbatch) {
+  try {
+    if (!mech) throw std::invalid_argument("null mechanism");
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return make_adjoint_plan(tables_for(mech, dev)->dev.L, nbatch, dev).bytes;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return 0;
+  }
+}
+
+int tchem_gb_adjoint(const tchem_gb_mech* mech, int nbatch, const double* tol_newton, const double* k_scale,
+                     const tchem_gb_tadv* tadv, const double* state, const double* tape_dt, const double* tape_ckpt,
+                     const int32_t* tape_nsteps, int tape_cap, const double* lambda, double* grad_x0, double* grad_k,
+                     int32_t* status, void* workspace, size_t workspace_bytes, void* stream_v) {
+  if (!mech || nbatch < 0) return fail(TCHEM_GB_ERR_ARG, "tchem_gb_adjoint: bad mechanism or batch size");
+  if (nbatch == 0) return TCHEM_GB_OK;
+  if (!tol_newton || !tadv || !state || !tape_dt || !tape_ckpt || !tape_nsteps || tape_cap < 1 || !lambda ||
+      !grad_x0 || !grad_k || !status)
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_adjoint: null argument or tape_cap < 1");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+  AdjointParams P{};
+  AdjointPlan a;
+  try {
+    const DeviceTables* t = tables_for(mech, dev);
+    if (!mech->host_tables->supported) throw std::domain_error(mech->host_tables->unsupported_reason);
+    a = make_adjoint_plan(t->dev.L, nbatch, dev);
+    P.mech = t->dev;
+    P.rate_param = t->dev.rate_param;
+  } catch (const std::domain_error& e) {
+    return fail(TCHEM_GB_ERR_UNSUPPORTED, e.what());
+  } catch (const std::exception& e) {
+    return fail(TCHEM_GB_ERR_ARG, e.what());
+  }
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  if (!ws) {
+    try {
+      ws = static_cast<unsigned char*>(owned_workspace(dev, a.bytes));
+    } catch (...) {
+      return fail(TCHEM_GB_ERR_NOMEM, "tchem_gb_adjoint: workspace allocation failed");
+    }
+  } else if (workspace_bytes < a.bytes) {
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_adjoint: workspace smaller than tchem_gb_adjoint_workspace_bytes()");
+  }
+  cudaError_t e = cudaMemsetAsync(ws, 0, 64, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(workspace)");
+  P.k_scale = k_scale;
+  P.B = nbatch;
+  P.state = state;
+  P.state_dim = mech->km.nSpec + 3;
+  P.tadv = tadv;
+  P.tol_newton = tol_newton;
+  P.tape_dt = tape_dt;
+  P.tape_ckpt = tape_ckpt;
+  P.tape_nsteps = tape_nsteps;
+  P.tape_cap = tape_cap;
+  P.lambda = lambda;
+  P.grad_x0 = grad_x0;
+  P.grad_k = grad_k;
+  P.status = status;
+  P.seg = reinterpret_cast<double*>(ws + a.seg_offset);
+  P.seg_stride = static_cast<int64_t>(a.seg_stride);
+  P.gmat = a.matrix_in_smem ? nullptr : reinterpret_cast<double*>(ws + a.gmat_offset);
+  P.gmat_stride = static_cast<int64_t>(a.gmat_stride);
+  P.lda = a.lda;
+  P.matrix_in_smem = a.matrix_in_smem ? 1 : 0;
+  P.warp_smem_bytes = static_cast<uint32_t>(a.warp_smem);
+  P.queue = reinterpret_cast<int32_t*>(ws);
+  P.error_word = reinterpret_cast<int32_t*>(ws + 64);
+  e = launch_adjoint(P, a.grid, a.warps, a.smem, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint kernel launch");
   return TCHEM_GB_OK;
 }
 

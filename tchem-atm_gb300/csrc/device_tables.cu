@@ -74,6 +74,16 @@ HostTables build_host_tables(const KineticModel& km) {
   if (m <= 0) throw std::runtime_error("mechanism has no active species");
   if (m >= 32768 || R >= 32768) throw std::runtime_error("mechanism too large for the device tables");
 
+  // Stoichiometry by reaction, as the reference stores it.
+  ht.rx_S = S;
+  ht.rx_sidx.assign(km.reacSidx.begin(), km.reacSidx.end());
+  ht.rx_nu.assign(km.reacNuki.begin(), km.reacNuki.end());
+  ht.rx_n.resize(static_cast<size_t>(R) * 2);
+  for (int r = 0; r < R; ++r) {
+    ht.rx_n[2 * r] = km.reacNreac[r];
+    ht.rx_n[2 * r + 1] = km.reacNprod[r];
+  }
+
   // Rate parameters per reaction.
   ht.rate_type.assign(R, RATE_ZERO);
   ht.rate_param.assign(static_cast<size_t>(R) * 8, 0.0);
@@ -290,6 +300,9 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   const size_t o_conv = sec(sizeof(int32_t) * R);
   const size_t o_cfp = sec(sizeof(int32_t) * (R + 1));
   const size_t o_cfi = sec(sizeof(int32_t) * std::max<size_t>(1, ht.cf_idx.size()));
+  const size_t o_rxs = sec(sizeof(int32_t) * ht.rx_sidx.size());
+  const size_t o_rxnu = sec(sizeof(double) * ht.rx_nu.size());
+  const size_t o_rxn = sec(sizeof(int32_t) * ht.rx_n.size());
   std::vector<unsigned char> host(off, 0);
   std::memcpy(host.data() + o_blob, ht.blob.data(), ht.blob.size());
   std::memcpy(host.data() + o_blob_x, ht.blob_x.data(), ht.blob_x.size());
@@ -298,6 +311,9 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   std::memcpy(host.data() + o_conv, ht.conv_exp.data(), sizeof(int32_t) * R);
   std::memcpy(host.data() + o_cfp, ht.cf_ptr.data(), sizeof(int32_t) * (R + 1));
   if (!ht.cf_idx.empty()) std::memcpy(host.data() + o_cfi, ht.cf_idx.data(), sizeof(int32_t) * ht.cf_idx.size());
+  std::memcpy(host.data() + o_rxs, ht.rx_sidx.data(), sizeof(int32_t) * ht.rx_sidx.size());
+  std::memcpy(host.data() + o_rxnu, ht.rx_nu.data(), sizeof(double) * ht.rx_nu.size());
+  std::memcpy(host.data() + o_rxn, ht.rx_n.data(), sizeof(int32_t) * ht.rx_n.size());
 
   int prev = 0;
   cudaGetDevice(&prev);
@@ -326,6 +342,10 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   t->dev.cf_ptr = reinterpret_cast<const int32_t*>(b + o_cfp);
   t->dev.cf_idx = reinterpret_cast<const int32_t*>(b + o_cfi);
   t->dev.conv_ppm = CONV_PPM;
+  t->dev.rx_sidx = reinterpret_cast<const int32_t*>(b + o_rxs);
+  t->dev.rx_nu = reinterpret_cast<const double*>(b + o_rxnu);
+  t->dev.rx_n = reinterpret_cast<const int32_t*>(b + o_rxn);
+  t->dev.rx_S = ht.rx_S;
   t->dev_x = t->dev;
   t->dev_x.L = ht.Lx;
   t->dev_x.blob = b + o_blob_x;

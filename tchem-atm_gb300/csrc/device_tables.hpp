@@ -55,6 +55,12 @@ struct MechDev {
   const int32_t* cf_ptr;      // [R+1] constant-species factors of reaction r
   const int32_t* cf_idx;      // constant-species slot (0..nconst-1), one entry per unit of |nu|
   double conv_ppm;
+  // Stoichiometry by reaction in the reference's layout (KineticModelNCAR_ConstData reacSidx,
+  // reacNuki, reacNreac, reacNprod): read by the adjoint for nu_r . mu.
+  const int32_t* rx_sidx;  // [R][rx_S]
+  const double* rx_nu;     // [R][rx_S], reactants signed negative, products from rx_S / 2
+  const int32_t* rx_n;     // [R][2]: number of reactants, products
+  int32_t rx_S;
 };
 
 // Host-side packed tables, built from a parsed kinetic model.
@@ -65,6 +71,9 @@ struct HostTables {
   std::vector<unsigned char> blob_x;
   std::vector<int32_t> rate_type, conv_exp, cf_ptr, cf_idx;
   std::vector<double> rate_param;
+  std::vector<int32_t> rx_sidx, rx_n;  // stoichiometry by reaction (MechDev::rx_*)
+  std::vector<double> rx_nu;
+  int32_t rx_S = 0;
   // Structural signature: mechanisms with equal signatures share one kernel launch.
   std::vector<int64_t> signature;
   bool supported = true;     // false when the mechanism has rate types outside the box path

@@ -13,6 +13,38 @@ cudaError_t launch_trbdf2_fp64(const AdvanceParams& P, int grid, int warps_per_b
                                cudaStream_t stream);
 const void* trbdf2_fp64_kernel_ptr(int m);
 
+// Discrete adjoint of the plain form (kernels_adjoint.cu): one warp per sample, one mechanism.
+struct AdjointParams {
+  MechDev mech;
+  const double* rate_param;
+  const double* k_scale;         // [R] rate-constant multipliers of the forward run, or null
+  int32_t B;
+  const double* state;           // [B][state_dim] initial states of the forward run
+  int32_t state_dim;
+  const tchem_gb_tadv* tadv;     // [B] (Newton settings)
+  const double* tol_newton;      // [2]
+  const double* tape_dt;         // [B][tape_cap]
+  const double* tape_ckpt;       // [B][tape_cap / kTapeSegment + 1][m]
+  const int32_t* tape_nsteps;    // [B]
+  int32_t tape_cap;
+  const double* lambda;          // [B][m] dL/dy(t_end)
+  double* grad_x0;               // [B][m] dL/dy(t_0)
+  double* grad_k;                // [B][R] dL/dtheta_r (k_r scaled by exp(theta_r))
+  int32_t* status;               // [B]
+  double* seg;                   // per warp: [kTapeSegment][2][m]
+  int64_t seg_stride;
+  double* gmat;                  // per-warp matrix slots when not in shared memory
+  int64_t gmat_stride;
+  int32_t lda;
+  int32_t matrix_in_smem;
+  uint32_t warp_smem_bytes;
+  int32_t* queue;
+  int32_t* error_word;
+};
+size_t adjoint_warp_smem_bytes(const MechLayout& L, int lda, bool matrix_in_smem);
+const void* adjoint_kernel_ptr(int m);
+cudaError_t launch_adjoint(const AdjointParams& P, int grid, int warps, size_t smem, cudaStream_t stream);
+
 // Unit kernels on the same tables (kernels_fp64.cu): one warp per sample.
 struct UnitParams {
   MechDev mech;

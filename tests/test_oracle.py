@@ -201,3 +201,35 @@ def test_step_budget_resumes_like_the_host_loop():
             break
     # Splitting the run into 50-step calls reproduces the single call exactly.
     np.testing.assert_array_equal(st, full[0])
+
+
+def test_adjoint_restatement_dot_product_and_finite_differences():
+    """The oracle's discrete adjoint against its forward sensitivities (dot-product test) and
+    central differences of the recorded-step replay."""
+    from oracle import binding as ob
+    km, state, tadv, tol_time = _generated_batch(2, seed=13)
+    tadv["tend"] = tadv["dtmax"] = 300.0
+    o = Oracle([km])
+    m, R = km.n_active, km.nReac
+    out, t, dt, st, tape = ob.record(o, tadv, state, [1e-18, 1e-8], tol_time, 2048)
+    assert np.all(st == 0) and np.all(t == 300.0)
+    assert np.allclose(tape.dt.sum(axis=1), 300.0, rtol=1e-12, atol=0)
+    y = out[:, 3:3 + m]
+    np.testing.assert_allclose(ob.replay(o, tadv, state, [1e-18, 1e-8], tape), y, rtol=0, atol=0)
+    tg = [2, 11, 30]
+    lam = np.zeros((2, m))
+    lam[:, tg] = 2 * np.log(y[:, tg]) / y[:, tg]
+    gx, gk = ob.adjoint(o, tadv, state, [1e-18, 1e-8], tape, lam)
+    rng = np.random.default_rng(2)
+    dx0, dth = rng.normal(size=(2, m)) * state[:, 3:3 + m], rng.normal(size=(2, R))
+    dy = ob.tangent(o, tadv, state, [1e-18, 1e-8], tape, dx0, dth)
+    lhs, rhs = (lam * dy).sum(axis=1), (gx * dx0).sum(axis=1) + (gk * dth).sum(axis=1)
+    assert (np.abs(lhs - rhs) / np.abs(lhs)).max() < 1e-10
+    h = 1e-6
+    for r in (4, 90):
+        ks = np.ones(R)
+        ks[r] = np.exp(h)
+        lp = (np.log(ob.replay(o, tadv, state, [1e-18, 1e-8], tape, ks)[:, tg]) ** 2).sum(axis=1)
+        ks[r] = np.exp(-h)
+        lm = (np.log(ob.replay(o, tadv, state, [1e-18, 1e-8], tape, ks)[:, tg]) ** 2).sum(axis=1)
+        assert np.abs((lp - lm) / (2 * h) - gk[:, r]).max() <= 1e-5 * np.abs(gk[:, r]).max() + 1e-12
