@@ -69,6 +69,8 @@ def parse() -> argparse.Namespace:
     ap.add_argument("--plain-samples", type=int, default=4096, help="subsample for the plain FP64 form")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of one oracle sample")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--adjoint-samples", type=int, default=8192,
+                    help="samples of the discrete-adjoint leg (1800 s horizon, FP64); 0 skips it")
     return ap.parse_args()
 
 
@@ -259,6 +261,52 @@ def reference_arm(args, world: int, rank: int):
     print(json.dumps(line), flush=True)
 
 
+# ---- discrete adjoint -------------------------------------------------------------------------
+
+def adjoint_leg(km, state, tol_time, n: int, dev, stream) -> dict:
+    """Forward (plain FP64, trajectory recorded) and adjoint times on the first n samples over an
+    1800 s horizon; the loss is the sum of squared log-ratios of 5 seeded target species."""
+    import torch
+    from tchem_gb import tadv_to_device
+    from tchem_gb import adjoint as adj
+    m = km.n_active
+    n = min(n, state.shape[0])
+    tadv = np.zeros(n, dtype=_capi.TIME_ADVANCE_DTYPE)
+    tadv["tbeg"], tadv["tend"], tadv["dt"], tadv["dtmin"], tadv["dtmax"] = 0.0, 1800.0, 1e-10, 1e-10, 1800.0
+    tadv["max_num_newton_iterations"] = 20
+    tadv["num_time_iterations_per_interval"] = 1_000_000
+    tadv["jacobian_interval"] = 1
+    d_tadv = tadv_to_device(tadv, dev)
+    d_state = torch.as_tensor(state[:n]).to(dev)
+    d_tn = torch.tensor(TOL_NEWTON, dtype=torch.float64, device=dev)
+    d_tt = torch.as_tensor(tol_time).to(dev)
+    out = torch.empty_like(d_state)
+    t = torch.zeros(n, dtype=torch.float64, device=dev)
+    dt = torch.zeros_like(t)
+    tape = adj.new_tape(n, m, 4096, dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    st = adj.record(km, d_tn, d_tt, d_tadv, d_state, t, dt, out, tape, stream=stream)
+    ev[1].record(stream)
+    y = out[:, 3:3 + m]
+    rng = np.random.default_rng(20251203)
+    tg = torch.as_tensor(rng.choice(m, 5, replace=False), device=dev)
+    ref = y[:, tg] * torch.exp(torch.as_tensor(rng.normal(0.0, 0.1, size=(n, 5)), device=dev))
+    lam = torch.zeros(n, m, dtype=torch.float64, device=dev)
+    lam[:, tg] = 2 * torch.log(y[:, tg] / ref) / y[:, tg]
+    ev[2].record(stream)
+    gx, gk, ast = adj.adjoint(km, d_tn, d_tadv, d_state, tape, lam, stream=stream)
+    ev[3].record(stream)
+    torch.cuda.synchronize(dev)
+    fwd = ev[0].elapsed_time(ev[1])
+    bwd = ev[2].elapsed_time(ev[3])
+    return {"samples": n, "horizon_s": 1800.0, "dtype": "f64", "checkpoint_every_steps": 32,
+            "forward_ms": fwd, "adjoint_ms": bwd, "adjoint_over_forward": bwd / fwd,
+            "failed_samples": int((st != 0).sum()) + int((ast != 0).sum()),
+            "mean_steps": float(tape.nsteps.double().mean()),
+            "gradients": "d loss / d ln A (156) and d loss / d ln x0 (51) per sample"}
+
+
 # ---- engine arm -------------------------------------------------------------------------------
 
 def engine_arm(args, world: int, rank: int, local: int):
@@ -374,6 +422,9 @@ def engine_arm(args, world: int, rank: int, local: int):
                                           f"over samples on {cores} threads ({el:.1f} s)"}
         line["accuracy_vs_fp64_oracle"] = {"samples": n, "max": float(e.max()), "p99": float(np.percentile(e, 99)),
                                            "floor": ATOL}
+
+    if rank == 0 and args.adjoint_samples > 0:
+        line["adjoint"] = adjoint_leg(km, state, tol_time, args.adjoint_samples, dev, stream)
 
     if not args.no_e2e:
         # end to end through the host-buffer C ABI: pinned host arrays in, results out, every copy
