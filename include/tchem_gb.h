@@ -184,6 +184,23 @@ int tchem_gb_time_advance_hostbuf(const tchem_gb_mech* const* mechs, int n_mechs
                                   double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats,
                                   const tchem_gb_advance_opts* opts, void* stream);
 
+/* tchem_gb_time_advance for callers that may not allocate device memory (no counterpart in the
+ * reference): a host model that owns every device allocation through its own pool, or a loop
+ * where cudaMalloc/cudaFree would synchronise the device. Same arguments as
+ * tchem_gb_time_advance without the workspace: the work-queue scratch is a fixed 1 MiB array
+ * inside the library (held by every device context that loads it). The mechanisms' device tables
+ * must already exist on the current device (call tchem_gb_workspace_bytes with them once at
+ * set-up); calls needing more scratch than 1 MiB (batches mixing mechanism structures need 4 bytes
+ * per sample and group) are rejected with TCHEM_GB_ERR_ARG. The first call on a device looks up
+ * the array's address: make it before any stream capture. All calls share the array: calls that
+ * overlap on the GPU race and must be serialised. Device-side wait timeouts are not reported
+ * through tchem_gb_device_error; samples no kernel reached keep the caller's status value. */
+int tchem_gb_time_advance_noalloc(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample,
+                                  int nbatch, const double* tol_newton, const double* tol_time, const double* fac,
+                                  const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
+                                  double* state_out, int32_t* status, tchem_gb_sample_stats* stats,
+                                  const tchem_gb_advance_opts* opts, void* stream);
+
 /* ---- Discrete adjoint (plain FP64 form, one mechanism) ------------------------------------
  * No counterpart in the reference (its TR-BDF2 has no adjoint); these extend runDeviceBatch
  * (src/core/TChem_AtmosphericChemistry.hpp:83-105) with the trajectory record and the
