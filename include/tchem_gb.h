@@ -132,7 +132,10 @@ int tchem_gb_scenario_read(const char* yaml_path, const tchem_gb_mech* mech, dou
 /* Numerical form of the time advance. */
 enum tchem_gb_form {
   TCHEM_GB_FORM_PLAIN_FP64 = 0, /* FP64 Newton LU: the parity form */
-  TCHEM_GB_FORM_MIXED = 1,      /* FP32 Newton LU and solves, FP64 residual/state/error control */
+  /* FP32 Newton LU and solves with one sweep of iterative refinement per Newton solve (FP64
+     residual of the linear system with the FP64 Jacobian, FP32 correction), FP64 Newton
+     residual, state and error control: follows the FP64 form's Newton iterates. */
+  TCHEM_GB_FORM_MIXED = 1,
   /* Simplified Newton with an FP32 Gauss-Jordan inverse of I - c J: the inverse is carried from
      the previous step's error filter while c changed by at most 30% (else formed at the first
      iterate) and reused by every Newton iteration of both stages; it is re-formed once per stage

@@ -83,7 +83,8 @@ class Oracle:
                      lu_fp32: int = 0, nthreads: int = 0, simplified: bool = False):
         """Returns (state_out, t_out, dt_out, status, stats).
 
-        lu_fp32: 0 FP64 LU; k >= 1 FP32 LU with k - 1 refinement sweeps after Newton convergence.
+        lu_fp32: 0 FP64 LU; k >= 1 FP32 LU with k - 1 refinement sweeps of every Newton linear solve
+        (k = 2 is the engine's mixed form).
         simplified: the simplified-Newton form (factors carried across iterations and steps).
         """
         B = state.shape[0]

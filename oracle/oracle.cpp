@@ -198,6 +198,7 @@ struct Sample {
   std::vector<double> kfor, rop, concX, J;
   DenseLU<LU_T> lu;
   tchem_gb_sample_stats st{};
+  std::vector<double> res, corr;  // refinement residual and correction
   // simplified-Newton form: factors valid / formed in the current stage, and their coefficient
   bool have_lu = false, fresh = false;
   double c_lu = 0.0;
@@ -217,6 +218,8 @@ struct Sample {
     if (k_scale)
       for (int r = 0; r < km.nReac; ++r) kfor[r] *= k_scale[r];
     lu.resize(m);
+    res.assign(m, 0.0);
+    corr.assign(m, 0.0);
   }
   void f(const double* y, double* out) {
     std::copy(y, y + m, concX.begin());
@@ -286,6 +289,19 @@ struct Sample {
       }
       lu.solve(g.data(), dx.data());
       ++st.n_solve;
+      // Iterative refinement of the linear solve: FP64 residual with the FP64 Jacobian the
+      // factors were built from, correction through the (FP32) factors.
+      for (int k = 0; k < s.refine; ++k) {
+        for (int i = 0; i < m; ++i) {
+          double jd = 0.0;
+          for (int j = 0; j < m; ++j) jd += J[static_cast<size_t>(i) * m + j] * dx[j];
+          res[i] = g[i] - (dx[i] - c * jd);
+        }
+        lu.solve(res.data(), corr.data());
+        ++st.n_solve;
+        ++st.n_rhs;  // the Jacobian-vector product, counted like a right-hand side
+        for (int i = 0; i < m; ++i) dx[i] += corr[i];
+      }
       ++st.n_newton_iter;
       double sdx = 0.0, sy = 0.0;
       for (int i = 0; i < m; ++i) {
@@ -295,17 +311,7 @@ struct Sample {
       }
       const double ndx = std::sqrt(sdx), ny = std::sqrt(sy);
       if (!std::isfinite(ndx) || !std::isfinite(ny)) return false;
-      if (ndx <= s.atol_newton + s.rtol_newton * ny) {
-        // Refinement sweeps of the mixed algorithm: FP64 residual, solve with the last factors.
-        for (int k = 0; k < s.refine; ++k) {
-          f(y, fy.data());
-          for (int i = 0; i < m; ++i) g[i] = -((y[i] - c * fy[i]) - rhs[i]);
-          lu.solve(g.data(), dx.data());
-          ++st.n_solve;
-          for (int i = 0; i < m; ++i) y[i] += dx[i];
-        }
-        return true;
-      }
+      if (ndx <= s.atol_newton + s.rtol_newton * ny) return true;
     }
     return false;
   }

@@ -43,8 +43,8 @@ int oracle_jacobian(const tchem_gb_kmcd_view* km, double T, double p, const doub
 /* Batched time advance with the reference's runDeviceBatch semantics on host arrays.
  * kms[n_mechs] with mech_of_sample[nbatch] (NULL: every sample uses kms[0]).
  * lu_fp32 = 0: FP64 Newton LU (the plain form); k >= 1: FP32 LU and solves with FP64 residuals
- * and k - 1 refinement sweeps after Newton convergence (the algorithm of the engine's
- * mixed-precision form, for like-for-like checks).
+ * and k - 1 sweeps of iterative refinement of every Newton linear solve (FP64 residual with the
+ * FP64 Jacobian, FP32 correction); k = 2 is the engine's mixed form.
  * simplified != 0: the simplified-Newton form of TCHEM_GB_FORM_MIXED_SIMPLIFIED (factors carried
  * across Newton iterations and steps, componentwise Newton test, error filter with I - c J(y_{n+1}));
  * the factors are LU here and a Gauss-Jordan inverse in the engine, which agree to the Newton

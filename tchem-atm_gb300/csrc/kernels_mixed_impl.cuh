@@ -40,7 +40,8 @@ namespace mixed {
 __host__ __device__ constexpr int ldu_for(int MC) { return (MC % 8 == 4) ? MC : MC + 4; }
 
 // Stage vectors kept in shared memory (FP64, [kVec][m]).
-// V_YP / V_YGP: y_n and y_gamma of the last accepted step (simplified form's stage-1 predictor).
+// V_YP / V_YGP: simplified form: y_n and y_gamma of the last accepted step (stage-1 predictor);
+// FP32-LU form: the refinement's vector and the point of the factored Jacobian.
 enum Vec { V_FN = 0, V_FG = 1, V_YP = 2, V_ATOL = 3, V_RTOL = 4, V_YGP = 5, kVec = 6 };
 // Work counters kept in shared memory, in tchem_gb_sample_stats order.
 enum Stat { S_STEPS = 0, S_REJ = 1, S_NFAIL = 2, S_NEWTON = 3, S_LU = 4, S_SOLVE = 5, S_RHS = 6, S_JAC = 7 };
@@ -152,6 +153,70 @@ struct Solver {
     __syncwarp();
 #pragma unroll
     for (int s = 0; s < RPT; ++s) f[s] = row(s) < L.m ? x[row(s)] : 0.0;
+    __syncwarp();
+    count(S_RHS);
+  }
+
+  // ---- FP64 Jacobian-vector product J(x_J) v (mixed form's refinement residual) ----------
+  // x_J: the point the factored matrix was built at (stage-vector slot V_YGP); v by row.
+  // dq_r/dx . v = keff_r sum_f v[sp_f] prod_{g != f} x[sp_g], then the net-production program
+  // without emissions.
+  __device__ __forceinline__ void jvec(const double (&v)[RPT], double (&out)[RPT]) {
+    const MechLayout& L = P.mech.L;
+    double* x = w<double>(P.ml.x);
+    double* vv = &vec(V_YP, 0);
+    double* q = w<double>(P.ml.q);
+    const double* keff = w<double>(P.ml.keff);
+#pragma unroll
+    for (int s = 0; s < RPT; ++s)
+      if (row(s) < L.m) {
+        x[row(s)] = vec(V_YGP, row(s));
+        vv[row(s)] = v[s];
+      }
+    __syncwarp();
+    const int32_t* rf_ptr = t<int32_t>(L.off_rf_ptr);
+    const int16_t* rf_sp = t<int16_t>(L.off_rf_sp);
+    for (int r = lane; r < L.R; r += 32) {
+      const int g0 = rf_ptr[r], g1 = rf_ptr[r + 1];
+      double dq = 0.0;
+      if (g1 - g0 == 1) {
+        dq = vv[rf_sp[g0]];
+      } else if (g1 - g0 == 2) {
+        const int a = rf_sp[g0], b = rf_sp[g0 + 1];
+        dq = vv[a] * x[b] + x[a] * vv[b];
+      } else {
+        for (int f = g0; f < g1; ++f) {
+          double p = vv[rf_sp[f]];
+          for (int g = g0; g < g1; ++g)
+            if (g != f) p *= x[rf_sp[g]];
+          dq += p;
+        }
+      }
+      q[r] = keff[r] * dq;
+    }
+    __syncwarp();
+    const int32_t* ws_sp = t<int32_t>(L.off_ws_sp);
+    const int32_t* ws_cnt = t<int32_t>(L.off_ws_cnt);
+    const int32_t* ws_off = t<int32_t>(L.off_ws_off);
+    const int16_t* wse_r = t<int16_t>(L.off_wse_r);
+    const double* wse_nu = t<double>(L.off_wse_nu);
+    for (int sl = 0; sl < L.NWS; ++sl) {
+      const int sp = ws_sp[sl * 32 + lane];
+      const int cnt = ws_cnt[sl];
+      const int base = ws_off[sl] + lane;
+      double a0 = 0.0, a1 = 0.0;
+      int c = 0;
+      for (; c + 2 <= cnt; c += 2) {
+        const int e = base + 32 * c;
+        a0 += wse_nu[e] * q[wse_r[e]];
+        a1 += wse_nu[e + 32] * q[wse_r[e + 32]];
+      }
+      if (c < cnt) a0 += wse_nu[base + 32 * c] * q[wse_r[base + 32 * c]];
+      if (sp >= 0) x[sp] = a0 + a1;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) out[s] = row(s) < L.m ? x[row(s)] : 0.0;
     __syncwarp();
     count(S_RHS);
   }
@@ -565,18 +630,33 @@ struct Solver {
   __device__ __forceinline__ bool newton(double (&y)[RPT], const double (&rv)[RPT], double coef, int max_newton,
                                          int jac_interval, double atol, double rtol) {
     for (int it = 0; it < max_newton; ++it) {
-      double f[RPT], dx[RPT];
+      double f[RPT], dx[RPT], g[RPT];
       float wf[RPT];
       rhs(y, f);
 #pragma unroll
-      for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(-((y[s] - coef * f[s]) - rv[s]));
+      for (int s = 0; s < RPT; ++s) {
+        g[s] = -((y[s] - coef * f[s]) - rv[s]);
+        wf[s] = static_cast<float>(g[s]);
+      }
       if (it % jac_interval == 0) {
         newton_matrix(y, coef);
+        put(V_YGP, y);  // the point of the factored Jacobian, for the refinement residual
         if (!factor_fwd(wf)) return false;
       } else {
         forward(wf);
       }
       backward(dx);
+      {
+        // one sweep of iterative refinement: FP64 residual of (I - c J) dx = g, FP32 correction
+        double jd[RPT], corr[RPT];
+        jvec(dx, jd);
+#pragma unroll
+        for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(g[s] - (dx[s] - coef * jd[s]));
+        forward(wf);
+        backward(corr);
+#pragma unroll
+        for (int s = 0; s < RPT; ++s) dx[s] += corr[s];
+      }
       count(S_NEWTON);
       double sdx = 0.0, sy = 0.0;
 #pragma unroll

@@ -243,7 +243,9 @@ def test_mixed_matches_fp64_oracle_on_cb05_shaped_batch(cfg1_like, form):
     assert np.all(st == 0)
     assert np.all(t == 3600.0) and np.all(dt == 0.0)
     err = rel_error(out[:, 3:3 + m], ref[0][:, 3:3 + m], ATOL_TIME)
-    assert err.max() <= 1e-6, err.max()
+    # the FP32-LU form refines every Newton solve with an FP64 residual, so it follows the FP64
+    # Newton iterates closely; the simplified form converges its own (different) iteration
+    assert err.max() <= (1e-7 if form == "mixed" else 1e-6), err.max()
     np.testing.assert_array_equal(out[:, :3], state[:, :3])
     # Neither the FP32 linear algebra nor the simplified Newton changes the step-size sequence
     # much: mean steps within 1 %.

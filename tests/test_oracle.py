@@ -147,6 +147,11 @@ def test_fp32_lu_mode_tracks_fp64():
     assert np.all(a[1] == 3600.0) and np.all(b[1] == 3600.0)
     err = rel_error(b[0][:, 3:3 + m], a[0][:, 3:3 + m], 1e-10)
     assert err.max() < 1e-5
+    # one FP64-residual refinement sweep per Newton solve (the engine's mixed form) follows the
+    # FP64 Newton iterates
+    c = o.time_advance(tadv, state, [1e-18, 1e-8], tol_time, lu_fp32=2)
+    assert rel_error(c[0][:, 3:3 + m], a[0][:, 3:3 + m], 1e-12).max() < 1e-7
+    np.testing.assert_array_equal(c[4]["n_steps"], a[4]["n_steps"])
 
 
 @pytest.mark.parametrize("lu_fp32", [0, 1])
