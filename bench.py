@@ -54,9 +54,10 @@ SEED = 7
 FORM_DTYPE = {"plain": "f64", "mixed": "f64 state / f32 LU + f64-residual refinement",
               "simplified": "f64 state / f32 Gauss-Jordan inverse"}
 # DRAM bytes per sample of the simplified-form kernel, from one ncu capture of a 4096-sample,
-# 600 s case (profiles/trbdf2_simplified_cb05_4096.md): the per-sample traffic (state in and out,
-# time-advance record, statistics) does not depend on the horizon.
-NCU_DRAM_BYTES_PER_SAMPLE = None
+# 600 s case (profiles/trbdf2_simplified_cb05_4096.md: 2,365,440 bytes read, 0 written -- the
+# results were still in L2 when the capture ended). The per-sample traffic (state, time-advance
+# record and times read once) does not depend on the horizon, so it scales by samples.
+NCU_DRAM_BYTES_PER_SAMPLE = {"simplified": 2365440 / 4096}
 
 
 def parse() -> argparse.Namespace:
@@ -375,7 +376,8 @@ def engine_arm(args, world: int, rank: int, local: int):
     L.tchem_gb_measure_fma_peak(0, 4, 65536, C.byref(peak32))
     ach64 = f64 / (kernel_ms * 1e-3) / 1e12
     ach32 = f32 / (kernel_ms * 1e-3) / 1e12
-    traffic = None if NCU_DRAM_BYTES_PER_SAMPLE is None else NCU_DRAM_BYTES_PER_SAMPLE * B
+    per_sample = NCU_DRAM_BYTES_PER_SAMPLE.get(args.form)
+    traffic = None if per_sample is None else per_sample * B
 
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
