@@ -151,7 +151,9 @@ enum tchem_gb_form {
 
 typedef struct tchem_gb_advance_opts {
   int32_t form;               /* tchem_gb_form */
-  int32_t threads_per_sample; /* 0: the tuned default for the mechanism */
+  int32_t threads_per_sample; /* mixed forms: 32, 64 or 128 threads (1, 2 or 4 warps) per sample;
+                                 0: the mechanism's tuned preference (tchem_gb_autotune), else the
+                                 narrowest kernel shape for its size */
   int32_t reserved[6];        /* zero */
 } tchem_gb_advance_opts;
 
@@ -233,6 +235,20 @@ int tchem_gb_adjoint(const tchem_gb_mech* mech, int nbatch, const double* tol_ne
                      const tchem_gb_tadv* tadv, const double* state, const double* tape_dt, const double* tape_ckpt,
                      const int32_t* tape_nsteps, int tape_cap, const double* lambda, double* grad_x0, double* grad_k,
                      int32_t* status, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Autotuner (no counterpart in the reference, whose team sizes are fixed at launch): times the
+ * form's kernel shapes (32, 64 and 128 threads per sample, where a shape exists for the
+ * mechanism's size) on a probe batch of device arrays laid out as for tchem_gb_time_advance
+ * (t_out is zeroed before every trial: the probe starts at t = 0; workspace may be NULL), keeps the
+ * fastest as the mechanism's preference for calls with opts.threads_per_sample == 0, and returns
+ * it in *chosen; ms_per_candidate[3] (optional) receives each trial's time (-1: not run).
+ * Synchronizes the stream. tchem_gb_mech_set_threads_per_sample sets the preference directly
+ * (0: the narrowest shape). */
+int tchem_gb_autotune(tchem_gb_mech* mech, int form, int nbatch, const double* tol_newton, const double* tol_time,
+                      const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
+                      double* state_out, int32_t* status, void* workspace, size_t workspace_bytes, void* stream,
+                      int* chosen, float* ms_per_candidate);
+int tchem_gb_mech_set_threads_per_sample(tchem_gb_mech* mech, int form, int threads_per_sample);
 
 /* Synchronizes `stream`, then reads and clears the device error word of `workspace` (NULL: the
  * library-owned workspace). *device_error is 0 when no kernel reported a timed-out wait. */

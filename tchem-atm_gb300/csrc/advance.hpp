@@ -16,7 +16,7 @@ constexpr int kTapeSegment = 32;    // steps between trajectory checkpoints (adj
 // kernel parameters (constant bank) so section addresses cost no registers.
 struct MixedLayout {
   uint32_t warp_bytes;
-  uint32_t x, keff, q, x32, keff32, d32, ustage, lrow, pinv, piv, ybuf, vec, stats, item;
+  uint32_t x, keff, q, x32, keff32, d32, ustage, lrow, pinv, piv, ybuf, vec, stats, red, item;
   int32_t LDU, LDL;
   int32_t simplified;  // 1: simplified-Newton form (Gauss-Jordan inverse, no L factor region)
 };

@@ -118,7 +118,9 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
     plan.m_max = std::max(plan.m_max, L.m);
     g.form = o.form;
     if (mixed) {
-      MixedConfig mc = mixed_config(L, o.threads_per_sample, info.sm_count, info.max_smem_optin, nbatch,
+      int tps = o.threads_per_sample;
+      if (tps == 0 && o.form >= 0 && o.form < 3) tps = mechs[g.mechs[0]]->tps_pref[o.form];
+      MixedConfig mc = mixed_config(L, tps, info.sm_count, info.max_smem_optin, nbatch,
                                     o.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED);
       g.kernel = mc.kernel;
       g.warps_per_block = mc.warps_per_block;
@@ -515,6 +517,70 @@ int tchem_gb_adjoint(const tchem_gb_mech* mech, int nbatch, const double* tol_ne
   P.error_word = reinterpret_cast<int32_t*>(ws + 64);
   e = launch_adjoint(P, a.grid, a.warps, a.smem, stream);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint kernel launch");
+  return TCHEM_GB_OK;
+}
+
+int tchem_gb_mech_set_threads_per_sample(tchem_gb_mech* mech, int form, int threads_per_sample) {
+  if (!mech || form < 0 || form > 2 ||
+      (threads_per_sample != 0 && threads_per_sample != 32 && threads_per_sample != 64 && threads_per_sample != 128))
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_mech_set_threads_per_sample: bad argument");
+  std::lock_guard<std::mutex> lk(mech->mu);
+  mech->tps_pref[form] = threads_per_sample;
+  return TCHEM_GB_OK;
+}
+
+int tchem_gb_autotune(tchem_gb_mech* mech, int form, int nbatch, const double* tol_newton, const double* tol_time,
+                      const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
+                      double* state_out, int32_t* status, void* workspace, size_t workspace_bytes, void* stream_v,
+                      int* chosen, float* ms_per_candidate) {
+  if (!mech || form < 0 || form > 2 || nbatch <= 0 || !chosen)
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_autotune: bad argument");
+  const int cands[3] = {32, 64, 128};
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess)
+    return fail(TCHEM_GB_ERR_CUDA, "tchem_gb_autotune: cudaEventCreate failed");
+  float best_ms = 0.f;
+  int best = 0;
+  const tchem_gb_mech* mechs[1] = {mech};
+  for (int c = 0; c < 3; ++c) {
+    if (ms_per_candidate) ms_per_candidate[c] = -1.f;
+    tchem_gb_advance_opts o{};
+    o.form = form;
+    o.threads_per_sample = cands[c];
+    if (form == TCHEM_GB_FORM_PLAIN_FP64 && cands[c] != 32) continue;  // the plain form has one shape
+    if (tchem_gb_workspace_bytes(mechs, 1, nbatch, &o) == 0) continue;  // no kernel of this shape
+    cudaMemsetAsync(t_out, 0, sizeof(double) * nbatch, stream);       // the probe starts at t = 0
+    cudaEventRecord(e0, stream);
+    const int rc = time_advance_impl(mechs, 1, nullptr, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out,
+                                     state_out, status, nullptr, workspace, workspace_bytes, &o, stream_v, TapeArgs{});
+    cudaEventRecord(e1, stream);
+    if (rc != TCHEM_GB_OK) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return rc;
+    }
+    if (cudaEventSynchronize(e1) != cudaSuccess) {
+      cudaEventDestroy(e0);
+      cudaEventDestroy(e1);
+      return fail(TCHEM_GB_ERR_CUDA, "tchem_gb_autotune: probe run failed");
+    }
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms_per_candidate) ms_per_candidate[c] = ms;
+    if (best == 0 || ms < best_ms) {
+      best = cands[c];
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best == 0) return fail(TCHEM_GB_ERR_UNSUPPORTED, "tchem_gb_autotune: no kernel shape for this mechanism");
+  {
+    std::lock_guard<std::mutex> lk(mech->mu);
+    mech->tps_pref[form] = best;
+  }
+  *chosen = best;
   return TCHEM_GB_OK;
 }
 

@@ -23,6 +23,8 @@ TCHEM_GB_DECLARE_SHAPE(simpl, 24, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 32, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 52, 2)
 TCHEM_GB_DECLARE_SHAPE(simpl, 64, 2)
+TCHEM_GB_DECLARE_SHAPE(simpl, 64, 1_g2)
+TCHEM_GB_DECLARE_SHAPE(simpl, 128, 1_g4)
 #undef TCHEM_GB_DECLARE_SHAPE
 
 namespace {
@@ -30,30 +32,38 @@ namespace {
 constexpr int kMaxWarps = 8;
 
 struct Variant {
-  int MC, RPT;
+  int MC, RPT, G;  // columns, rows per thread, warps per sample
   bool simplified;
   const void* kernel;
   cudaError_t (*launch)(const AdvanceParams&, int, int, size_t, cudaStream_t);
 };
 
-// Kernel shapes (columns, rows per lane) of each form; a mechanism uses the narrowest with
-// MC >= m and 32 * RPT >= m.
+// Kernel shapes of each form; a mechanism uses the narrowest with MC >= m and 32 G RPT >= m,
+// among those with the requested threads per sample (32 G; 0: any, fewest warps first).
 const Variant* variants(int* n) {
   static const Variant v[] = {
-      {24, 1, false, kernel_mixed_24_1(), &launch_mixed_24_1}, {32, 1, false, kernel_mixed_32_1(), &launch_mixed_32_1},
-      {52, 2, false, kernel_mixed_52_2(), &launch_mixed_52_2}, {64, 2, false, kernel_mixed_64_2(), &launch_mixed_64_2},
-      {24, 1, true, kernel_simpl_24_1(), &launch_simpl_24_1},  {32, 1, true, kernel_simpl_32_1(), &launch_simpl_32_1},
-      {52, 2, true, kernel_simpl_52_2(), &launch_simpl_52_2},  {64, 2, true, kernel_simpl_64_2(), &launch_simpl_64_2},
+      {24, 1, 1, false, kernel_mixed_24_1(), &launch_mixed_24_1},
+      {32, 1, 1, false, kernel_mixed_32_1(), &launch_mixed_32_1},
+      {52, 2, 1, false, kernel_mixed_52_2(), &launch_mixed_52_2},
+      {64, 2, 1, false, kernel_mixed_64_2(), &launch_mixed_64_2},
+      {24, 1, 1, true, kernel_simpl_24_1(), &launch_simpl_24_1},
+      {32, 1, 1, true, kernel_simpl_32_1(), &launch_simpl_32_1},
+      {52, 2, 1, true, kernel_simpl_52_2(), &launch_simpl_52_2},
+      {64, 2, 1, true, kernel_simpl_64_2(), &launch_simpl_64_2},
+      {64, 1, 2, true, kernel_simpl_64_1_g2(), &launch_simpl_64_1_g2},
+      {128, 1, 4, true, kernel_simpl_128_1_g4(), &launch_simpl_128_1_g4},
   };
   *n = static_cast<int>(sizeof(v) / sizeof(v[0]));
   return v;
 }
 
-const Variant* pick(const MechLayout& L, bool simplified) {
+const Variant* pick(const MechLayout& L, bool simplified, int threads_per_sample) {
   int nv = 0;
   const Variant* v = variants(&nv);
   for (int i = 0; i < nv; ++i)
-    if (v[i].simplified == simplified && v[i].MC >= L.m && 32 * v[i].RPT >= L.m) return &v[i];
+    if (v[i].simplified == simplified && v[i].MC >= L.m && 32 * v[i].G * v[i].RPT >= L.m &&
+        (threads_per_sample == 0 || threads_per_sample == 32 * v[i].G))
+      return &v[i];
   return nullptr;
 }
 
@@ -61,33 +71,37 @@ const Variant* pick(const MechLayout& L, bool simplified) {
 
 MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch,
                          bool simplified) {
-  if (threads_per_sample != 0 && threads_per_sample != 32)
-    throw std::domain_error("mixed form: threads_per_sample must be 0 or 32");
-  const Variant* best = pick(L, simplified);
-  if (!best) throw std::domain_error("mixed form: mechanisms with more than 64 active species are not supported");
+  if (threads_per_sample != 0 && threads_per_sample != 32 && threads_per_sample != 64 && threads_per_sample != 128)
+    throw std::domain_error("mixed forms: threads_per_sample must be 0, 32, 64 or 128");
+  const Variant* best = pick(L, simplified, threads_per_sample);
+  if (!best)
+    throw std::domain_error(simplified ? "simplified form: no kernel shape for this mechanism size and threads_per_sample "
+                                         "(up to 64 species with 32 or 64 threads, 128 with 128 threads)"
+                                       : "FP32-LU form: mechanisms with more than 64 active species are not supported");
   const MixedLayout ml = mixed::make_layout(L, best->MC, simplified);
   const size_t gbytes = ml.warp_bytes;
   const size_t avail = static_cast<size_t>(max_smem_optin) - 16 - L.blob_bytes;
-  const int warps = static_cast<int>(std::min<size_t>(kMaxWarps, avail / gbytes));
-  if (warps < 1) throw std::domain_error("mixed form: shared-memory working set too large");
+  const int groups = static_cast<int>(std::min<size_t>(kMaxWarps / best->G, avail / gbytes));
+  if (groups < 1) throw std::domain_error("mixed form: shared-memory working set too large");
+  const int warps = groups * best->G;
   MixedConfig mc;
   mc.kernel = best->kernel;
-  mc.threads_per_sample = 32;
+  mc.threads_per_sample = 32 * best->G;
   mc.ml = ml;
   mc.warps_per_block = warps;
-  mc.smem = 16 + L.blob_bytes + warps * gbytes;
+  mc.smem = 16 + L.blob_bytes + groups * gbytes;
   cudaFuncSetAttribute(mc.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(mc.smem));
   int bps = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, mc.kernel, warps * 32, mc.smem) != cudaSuccess || bps < 1)
     bps = 1;
-  const int need = (std::max(nbatch, 1) + warps - 1) / warps;
+  const int need = (std::max(nbatch, 1) + groups - 1) / groups;
   mc.grid = std::max(1, std::min(sm_count * bps, need));
   return mc;
 }
 
 cudaError_t launch_trbdf2_mixed(const AdvanceParams& P, const MechLayout& L, int grid, int warps_per_block,
-                                size_t smem, int /*threads_per_sample*/, cudaStream_t stream) {
-  const Variant* best = pick(L, P.ml.simplified != 0);
+                                size_t smem, int threads_per_sample, cudaStream_t stream) {
+  const Variant* best = pick(L, P.ml.simplified != 0, threads_per_sample);
   if (!best) return cudaErrorInvalidValue;
   return best->launch(P, grid, warps_per_block * 32, smem, stream);
 }

@@ -67,6 +67,7 @@ inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified) {
   ml.piv = o; o += up16(sizeof(int) * L.m);
   ml.ybuf = o; o += up16(sizeof(float) * MC);  // MC >= m
   ml.stats = o; o += up16(sizeof(int) * 8);
+  ml.red = o; o += 256;  // cross-warp reductions of multi-warp samples (2 x 8 u32, 2 x 8 f64, 2 f32)
   ml.item = o; o += up16(sizeof(int) * 4);
   ml.warp_bytes = o;
   return ml;
@@ -74,15 +75,29 @@ inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified) {
 
 // SIMP selects the simplified-Newton form (Gauss-Jordan inverse); each form is its own kernel so
 // that neither carries the other's code through the instruction cache.
-template <int MC, int RPT, bool SIMP>
+//
+// G > 1 (simplified form only) spreads one sample over G warps of one CTA, one row per thread:
+// loops stride over the group's 32 G threads, the sliced-ELL programs go slice by slice to the
+// group's warps, and reductions and the pivot broadcast go through shared memory with a named
+// barrier per group.
+template <int MC, int RPT, bool SIMP, int G = 1>
 struct Solver {
   static_assert(MC % 4 == 0, "MC must be a multiple of 4");
+  static_assert(G == 1 || (SIMP && RPT == 1), "multi-warp samples: simplified form, one row per thread");
   static constexpr int LDU = ldu_for(MC);
+  static constexpr int NT = 32 * G;                       // threads per sample
+  static constexpr int NROWS = NT * RPT;                  // rows held in registers
+  static_assert(NROWS <= 128, "row index must fit the pivot key");
+  static constexpr uint32_t KMASK = NROWS <= 64 ? 63u : 127u;  // low key bits holding the row
 
   const AdvanceParams& P;
   const unsigned char* tb;  // staged tables
-  unsigned char* wb;        // this warp's region
-  int lane;
+  unsigned char* wb;        // this sample's region
+  int lane;                 // lane in the warp
+  int tid;                  // thread in the sample's group (== lane for G == 1)
+  int wid;                  // warp in the group
+  int bar;                  // named barrier of the group (G > 1)
+  int rp = 0;               // rotating slot of the cross-warp reductions
 
   float A[RPT][MC];  // active rows, shifted: register j holds column k + j at step k
   int step[RPT];     // step at which the row became the pivot (INT_MAX while active)
@@ -92,14 +107,84 @@ struct Solver {
   double c_inv = 0.0;
 
   __device__ __forceinline__ int m() const { return P.mech.L.m; }
-  __device__ __forceinline__ int row(int s) const { return lane + 32 * s; }
+  // thread index in the sample's group (the lane itself for one warp per sample)
+  __device__ __forceinline__ int gt() const {
+    if constexpr (G == 1) {
+      return lane;
+    } else {
+      return tid;
+    }
+  }
+  __device__ __forceinline__ int row(int s) const {
+    if constexpr (G == 1) {
+      return lane + 32 * s;
+    } else {
+      return tid + NT * s;
+    }
+  }
   template <typename Tp>
   __device__ __forceinline__ Tp* w(uint32_t off) const { return reinterpret_cast<Tp*>(wb + off); }
   template <typename Tp>
   __device__ __forceinline__ const Tp* t(int32_t off) const { return reinterpret_cast<const Tp*>(tb + off); }
   __device__ __forceinline__ double& vec(int v, int i) const { return w<double>(P.ml.vec)[v * m() + i]; }
   __device__ __forceinline__ void count(int which) const {
-    if (lane == 0) ++w<int>(P.ml.stats)[which];
+    if (gt() == 0) ++w<int>(P.ml.stats)[which];
+  }
+
+  // ---- group synchronisation and reductions (G == 1: warp primitives) -----------------------
+  __device__ __forceinline__ void gsync() const {
+    if constexpr (G == 1) {
+      __syncwarp();
+    } else {
+      asm volatile("bar.sync %0, %1;" ::"r"(bar), "r"(NT) : "memory");
+    }
+  }
+  // Every cross-warp reduction passes one barrier; two rotating slots keep a warp that runs
+  // ahead from overwriting values a slower warp has not read yet.
+  __device__ __forceinline__ uint32_t gmax_u32(uint32_t v) {
+    v = __reduce_max_sync(kFullMask, v);
+    if constexpr (G == 1) {
+      return v;
+    } else {
+      uint32_t* r = w<uint32_t>(P.ml.red) + 8 * rp;
+      rp ^= 1;
+      if (lane == 0) r[wid] = v;
+      gsync();
+      uint32_t mx = r[0];
+#pragma unroll
+      for (int i = 1; i < G; ++i) mx = max(mx, r[i]);
+      return mx;
+    }
+  }
+  __device__ __forceinline__ uint32_t gor_u32(uint32_t v) {
+    v = __reduce_or_sync(kFullMask, v);
+    if constexpr (G == 1) {
+      return v;
+    } else {
+      uint32_t* r = w<uint32_t>(P.ml.red) + 8 * rp;
+      rp ^= 1;
+      if (lane == 0) r[wid] = v;
+      gsync();
+      uint32_t o = r[0];
+#pragma unroll
+      for (int i = 1; i < G; ++i) o |= r[i];
+      return o;
+    }
+  }
+  __device__ __forceinline__ double gmax_f64(double v) {
+    v = warp_max(v);
+    if constexpr (G == 1) {
+      return v;
+    } else {
+      double* r = reinterpret_cast<double*>(w<unsigned char>(P.ml.red) + 64) + 8 * rp;
+      rp ^= 1;
+      if (lane == 0) r[wid] = v;
+      gsync();
+      double mx = r[0];
+#pragma unroll
+      for (int i = 1; i < G; ++i) mx = fmax(mx, r[i]);
+      return mx;
+    }
   }
 
   // ---- FP64 right-hand side: src/core/impl/TChem_Impl_ReactionRatesAerosol.hpp:80-138 -----
@@ -112,11 +197,11 @@ struct Solver {
 #pragma unroll
     for (int s = 0; s < RPT; ++s)
       if (row(s) < L.m) x[row(s)] = y[s];
-    __syncwarp();
+    gsync();
     const int32_t* rf_ptr = t<int32_t>(L.off_rf_ptr);
     const int16_t* rf_sp = t<int16_t>(L.off_rf_sp);
 #pragma unroll 2
-    for (int r = lane; r < L.R; r += 32) {
+    for (int r = gt(); r < L.R; r += NT) {
       const int g0 = rf_ptr[r], g1 = rf_ptr[r + 1];
       double qq = keff[r];
       if (g1 > g0) qq *= x[rf_sp[g0]];
@@ -124,7 +209,7 @@ struct Solver {
       for (int g = g0 + 2; g < g1; ++g) qq *= x[rf_sp[g]];
       q[r] = qq;
     }
-    __syncwarp();
+    gsync();
     // net production over species slices (sliced ELL); results staged in x by species
     const int32_t* ws_sp = t<int32_t>(L.off_ws_sp);
     const int32_t* ws_cnt = t<int32_t>(L.off_ws_cnt);
@@ -133,7 +218,7 @@ struct Solver {
     const double* wse_nu = t<double>(L.off_wse_nu);
     const double* emis = t<double>(L.off_emis);
 #pragma unroll 2
-    for (int sl = 0; sl < L.NWS; ++sl) {
+    for (int sl = wid; sl < L.NWS; sl += G) {
       const int sp = ws_sp[sl * 32 + lane];
       const int cnt = ws_cnt[sl];
       const int base = ws_off[sl] + lane;
@@ -150,10 +235,10 @@ struct Solver {
       for (; c < cnt; ++c) a0 += wse_nu[base + 32 * c] * q[wse_r[base + 32 * c]];
       if (sp >= 0) x[sp] = emis[sp] + ((a0 + a1) + (a2 + a3));
     }
-    __syncwarp();
+    gsync();
 #pragma unroll
     for (int s = 0; s < RPT; ++s) f[s] = row(s) < L.m ? x[row(s)] : 0.0;
-    __syncwarp();
+    gsync();
     count(S_RHS);
   }
 
@@ -162,6 +247,7 @@ struct Solver {
   // dq_r/dx . v = keff_r sum_f v[sp_f] prod_{g != f} x[sp_g], then the net-production program
   // without emissions.
   __device__ __forceinline__ void jvec(const double (&v)[RPT], double (&out)[RPT]) {
+    static_assert(G == 1, "FP32-LU form: one warp per sample");
     const MechLayout& L = P.mech.L;
     double* x = w<double>(P.ml.x);
     double* vv = &vec(V_YP, 0);
@@ -233,7 +319,7 @@ struct Solver {
     for (int s = 0; s < RPT; ++s)
       if (row(s) < mm) x32[row(s)] = static_cast<float>(y[s]);
     // identity rows into the staging matrix (columns >= m stay 0)
-    for (int e = lane; e < mm * (LDU / 4); e += 32) {
+    for (int e = gt(); e < mm * (LDU / 4); e += NT) {
       const int i = e / (LDU / 4), j4 = (e - i * (LDU / 4)) * 4;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
       if (i == j4) v.x = 1.f;
@@ -242,11 +328,11 @@ struct Solver {
       if (i == j4 + 3) v.w = 1.f;
       reinterpret_cast<float4*>(stage + i * LDU)[j4 / 4] = v;
     }
-    __syncwarp();
+    gsync();
     const int32_t* rf_ptr = t<int32_t>(L.off_rf_ptr);
     const int16_t* rf_sp = t<int16_t>(L.off_rf_sp);
 #pragma unroll 2
-    for (int r = lane; r < L.R; r += 32) {
+    for (int r = gt(); r < L.R; r += NT) {
       const int f0 = rf_ptr[r], f1 = rf_ptr[r + 1];
       const float kr = keff32[r];
       if (f1 - f0 == 1) {
@@ -264,7 +350,7 @@ struct Solver {
         }
       }
     }
-    __syncwarp();
+    gsync();
     const float c = static_cast<float>(coef);
     const int32_t* js_rc = t<int32_t>(L.off_js_rc);
     const int32_t* js_cnt = t<int32_t>(L.off_js_cnt);
@@ -273,7 +359,7 @@ struct Solver {
     const float* jse_nu = t<float>(L.off_jse_nu32);
     // Jacobian nonzeros over slices (sliced ELL): uniform trip counts, independent loads
 #pragma unroll 2
-    for (int sl = 0; sl < L.NJS; ++sl) {
+    for (int sl = wid; sl < L.NJS; sl += G) {
       const int rc = js_rc[sl * 32 + lane];
       const int cnt = js_cnt[sl];
       const int base = js_off[sl] + lane;
@@ -291,7 +377,7 @@ struct Solver {
         stage[i * LDU + j] = (i == j ? 1.f : 0.f) - c * (J0 + J1);
       }
     }
-    __syncwarp();
+    gsync();
 #pragma unroll
     for (int s = 0; s < RPT; ++s) {
       const int i = row(s);
@@ -310,7 +396,7 @@ struct Solver {
         for (int j = 0; j < MC; ++j) A[s][j] = 0.f;
       }
     }
-    __syncwarp();  // the staging area is overwritten by the U rows from here on
+    gsync();  // the staging area is overwritten by the U rows from here on
     count(S_JAC);
   }
 
@@ -342,7 +428,7 @@ struct Solver {
     uint32_t key = 0u;
 #pragma unroll
     for (int s = 0; s < RPT; ++s) {
-      const uint32_t kb = ((__float_as_uint(A[s][0]) & 0x7fffffffu) & ~63u) | static_cast<uint32_t>(63 - row(s));
+      const uint32_t kb = ((__float_as_uint(A[s][0]) & 0x7fffffffu) & ~KMASK) | (KMASK - static_cast<uint32_t>(row(s)));
       key = max(key, act[s] ? kb : 0u);
     }
     return key;
@@ -380,6 +466,7 @@ struct Solver {
   // the next step's pivot reduction is issued as soon as the first column group is updated, so
   // its latency overlaps the rest of the update.
   __device__ __forceinline__ bool factor_fwd(float (&wf)[RPT]) {
+    static_assert(G == 1, "FP32-LU form: one warp per sample");
     static_assert(32 * RPT <= 64, "row index must fit the 6 key bits");
     constexpr int NG = MC / 4;
     constexpr int C1 = (NG + 2) / 3, C2 = (2 * NG + 2) / 3;
@@ -463,7 +550,6 @@ struct Solver {
   // to ustage (row-major by physical row) for apply_inverse. Returns false on a zero or
   // non-finite pivot.
   __device__ __forceinline__ bool invert() {
-    static_assert(32 * RPT <= 64, "row index must fit the 6 key bits");
     constexpr int NG = MC / 4;
     const int mm = m();
     float* ustage = w<float>(P.ml.ustage);
@@ -475,20 +561,29 @@ struct Solver {
       step[s] = INT_MAX;
       pr[s] = 0.f;
     }
-    uint32_t gk = __reduce_max_sync(kFullMask, pivot_key(act));
+    uint32_t gk = gmax_u32(pivot_key(act));
 #pragma unroll 1
     for (int k = 0; k < mm; ++k) {
-      if ((gk >> 6) == 0u || (gk & ~63u) >= 0x7f800000u) return false;  // zero column, inf or nan
-      const int p = 63 - static_cast<int>(gk & 63u);
-      const int owner = p & 31, pslot = p >> 5;
-      const bool is_owner = lane == owner;
+      if ((gk & ~KMASK) == 0u || (gk & ~KMASK) >= 0x7f800000u) return false;  // zero column, inf or nan
+      const int p = static_cast<int>(KMASK - (gk & KMASK));
+      const int owner = p % NT, pslot = p / NT;
+      const bool is_owner = gt() == owner;
       float pv_mine = A[0][0];
 #pragma unroll
       for (int s = 1; s < RPT; ++s)
         if (pslot == s) pv_mine = A[s][0];
       float* urow = ustage + k * LDU;
       publish_row(urow, pslot, is_owner);
-      const float pinv = __fdividef(1.f, __shfl_sync(kFullMask, pv_mine, owner));
+      float pval;
+      if constexpr (G == 1) {
+        pval = __shfl_sync(kFullMask, pv_mine, owner);
+      } else {
+        float* pvb = reinterpret_cast<float*>(w<unsigned char>(P.ml.red) + 192);
+        if (is_owner) pvb[k & 1] = pv_mine;
+        gsync();  // the pivot value and the published row are visible to the group
+        pval = pvb[k & 1];
+      }
+      const float pinv = __fdividef(1.f, pval);
       float l[RPT], ext[RPT];
 #pragma unroll
       for (int s = 0; s < RPT; ++s) {
@@ -501,15 +596,16 @@ struct Solver {
         l[s] = piv_row ? 0.f : A[s][0] * pinv;
         ext[s] = piv_row ? 1.f : -l[s];
       }
-      __syncwarp();
+      if constexpr (G == 1) __syncwarp();
       update_chunk<0, 1>(l, urow, ext);
-      gk = __reduce_max_sync(kFullMask, pivot_key(act));
+      gk = gmax_u32(pivot_key(act));
       constexpr int C1 = (NG + 2) / 3, C2 = (2 * NG + 2) / 3;
       update_chunk<1, C1>(l, urow, ext);
       update_chunk<C1, C2>(l, urow, ext);
       update_chunk<C2, NG>(l, urow, ext);
-      __syncwarp();
+      if constexpr (G == 1) __syncwarp();
     }
+    if constexpr (G > 1) gsync();  // every warp is done reading the pivot rows
     // scaled rows to ustage (the pivot-row copies above are no longer needed)
 #pragma unroll
     for (int s = 0; s < RPT; ++s) {
@@ -521,7 +617,7 @@ struct Solver {
                                A[s][4 * g + 3] * pr[s]);
       }
     }
-    __syncwarp();
+    gsync();
     count(S_LU);
     return true;
   }
@@ -538,7 +634,7 @@ struct Solver {
 #pragma unroll
     for (int s = 0; s < RPT; ++s)
       if (row(s) < mm) gs[off + step[s]] = gf[s];
-    __syncwarp();
+    gsync();
     float a0[RPT], a1[RPT], a2[RPT], a3[RPT];
 #pragma unroll
     for (int s = 0; s < RPT; ++s) a0[s] = a1[s] = a2[s] = a3[s] = 0.f;
@@ -556,20 +652,21 @@ struct Solver {
         }
       }
     }
-    __syncwarp();
+    gsync();
 #pragma unroll
     for (int s = 0; s < RPT; ++s)
       if (row(s) < mm) xs[step[s]] = (a0[s] + a1[s]) + (a2[s] + a3[s]);
-    __syncwarp();
+    gsync();
 #pragma unroll
     for (int s = 0; s < RPT; ++s) x[s] = row(s) < mm ? static_cast<double>(xs[row(s)]) : 0.0;
-    __syncwarp();
+    gsync();
     count(S_SOLVE);
   }
 
   // Forward substitution with the stored multipliers (rows' values in wf, in place); leaves the
   // values in step order in ybuf.
   __device__ __forceinline__ void forward(float (&wf)[RPT]) {
+    static_assert(G == 1, "FP32-LU form: one warp per sample");
     const int mm = m();
     const float* lrow = w<float>(P.ml.lrow);
     const int* piv = w<int>(P.ml.piv);
@@ -712,11 +809,12 @@ struct Solver {
           dbits = max(dbits, __float_as_uint(static_cast<float>(fabs(dx[s]))));
         }
       }
-      if (!__all_sync(kFullMask, finite)) return false;
-      const float dmax = __uint_as_float(__reduce_max_sync(kFullMask, dbits));
+      const uint32_t flags = gor_u32((finite ? 0u : 1u) | (conv ? 0u : 2u));
+      if (flags & 1u) return false;
+      const float dmax = __uint_as_float(gmax_u32(dbits));
       if (it > 0 && !fresh && dmax > 0.5f * prev) refresh = true;
       prev = dmax;
-      if (__all_sync(kFullMask, conv)) return true;
+      if (!(flags & 2u)) return true;
     }
     return false;
   }
@@ -855,7 +953,7 @@ struct Solver {
           err = fmax(err, fabs(estf[s]) / wgt);
         }
       }
-      err = warp_max(err);
+      err = gmax_f64(err);
       if (!isfinite(err)) { status = TCHEM_GB_SAMPLE_NONFINITE; break; }
       if (err <= 1.0 || dt <= dt_min) {
         t = last ? t_end : t + dt;
@@ -877,7 +975,7 @@ struct Solver {
         count(S_REJ);
         dt *= fmax(0.2, 0.9 * cbrt(1.0 / err));
       }
-      __syncwarp();
+      gsync();
     }
     t_out = t;
     dt_out = dt;
@@ -891,8 +989,9 @@ struct Solver {
   }
 };
 
-// One warp per sample, persistent work queue (same outer protocol as the plain kernel).
-template <int MC, int RPT, bool SIMP>
+// One sample per group of G warps (G = 1: one warp), persistent work queue (same outer protocol as
+// the plain kernel).
+template <int MC, int RPT, bool SIMP, int G>
 __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_constant__ AdvanceParams P) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
@@ -902,8 +1001,10 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
     if (threadIdx.x == 0) atomicOr(P.error_word, kErrBarrierTimeout);
     return;
   }
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  Solver<MC, RPT, SIMP> S{P, tables, tables + L.blob_bytes + warp * P.ml.warp_bytes, lane};
+  constexpr int NT = 32 * G;
+  const int group = threadIdx.x / NT, tid = threadIdx.x % NT, lane = threadIdx.x & 31;
+  Solver<MC, RPT, SIMP, G> S{P, tables, tables + L.blob_bytes + group * P.ml.warp_bytes, lane, tid, tid >> 5,
+                             1 + group};
   const int m = L.m;
   const int n_items = P.n_items_dev ? *P.n_items_dev : P.n_items;
   int* stats = S.template w<int>(P.ml.stats);
@@ -912,15 +1013,15 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
   int* item_s = S.template w<int>(P.ml.item);
 
   while (true) {
-    if (lane == 0) item_s[0] = atomicAdd(P.queue, 1);
-    __syncwarp();
+    if (tid == 0) item_s[0] = atomicAdd(P.queue, 1);
+    S.gsync();
     const int item = item_s[0];
-    __syncwarp();
+    S.gsync();
     if (item >= n_items) break;
     const int smp = P.items ? P.items[item] : item;
     const tchem_gb_tadv ta = P.tadv[smp];
     if (P.t_out[smp] >= ta.tend) {
-      if (lane == 0) {
+      if (tid == 0) {
         P.status[smp] = TCHEM_GB_SAMPLE_SKIPPED;
         if (P.stats) P.stats[smp] = tchem_gb_sample_stats{};
       }
@@ -929,7 +1030,7 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
     const int gm = P.mech_of_sample ? P.mech_of_sample[smp] : 0;
     const int slot = (gm >= 0 && gm < kMaxMechs) ? P.slot_of_mech[gm] : -1;
     if (slot < 0) {
-      if (lane == 0) P.status[smp] = TCHEM_GB_SAMPLE_BAD_MECH;
+      if (tid == 0) P.status[smp] = TCHEM_GB_SAMPLE_BAD_MECH;
       continue;
     }
     const double* row = P.state + static_cast<size_t>(smp) * P.state_dim;
@@ -938,26 +1039,26 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
       const double t_1 = 1.0 / Tk;
       const double conv = P.mech.conv_ppm * p * t_1;
       const double* rp = P.rate_param[slot];
-      for (int r = lane; r < L.R; r += 32) {
+      for (int r = tid; r < L.R; r += NT) {
         double k = rate_constant(P.mech.rate_type[r], rp + 8 * r, P.mech.conv_exp[r], Tk, t_1, p, conv);
         for (int c = P.mech.cf_ptr[r]; c < P.mech.cf_ptr[r + 1]; ++c) k *= row[3 + m + P.mech.cf_idx[c]];
         keff[r] = k;
         keff32[r] = static_cast<float>(k);
       }
     }
-    for (int i = lane; i < m; i += 32) {
+    for (int i = tid; i < m; i += NT) {
       S.vec(V_ATOL, i) = P.tol_time[2 * i];
       S.vec(V_RTOL, i) = P.tol_time[2 * i + 1];
     }
-    if (lane < 8) stats[lane] = 0;
-    if (lane == 0) {
+    if (tid < 8) stats[tid] = 0;
+    if (tid == 0) {
       S.template w<double>(P.ml.q)[L.R] = 0.0;
       S.template w<float>(P.ml.d32)[L.NF] = 0.f;
     }
     if constexpr (SIMP)
-      for (int j = lane; j < MC; j += 32) S.template w<float>(P.ml.ybuf)[j] = 0.f;  // leading zeros of apply_inverse
+      for (int j = tid; j < MC; j += NT) S.template w<float>(P.ml.ybuf)[j] = 0.f;  // leading zeros of apply_inverse
     S.have_inv = false;
-    __syncwarp();
+    S.gsync();
     double y[RPT];
 #pragma unroll
     for (int s = 0; s < RPT; ++s) {
@@ -968,8 +1069,8 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
     const int jac_int = ta.jacobian_interval > 0 ? ta.jacobian_interval : 1;
     const int stt = S.integrate(y, ta.tbeg, ta.tend, ta.dt, ta.dtmin, ta.dtmax, ta.num_time_iterations_per_interval,
                                 ta.max_num_newton_iterations, jac_int, P.tol_newton[0], P.tol_newton[1], t_o, dt_o);
-    __syncwarp();
-    if (lane == 0) {
+    S.gsync();
+    if (tid == 0) {
       P.status[smp] = stt;
       if (P.stats) {
         tchem_gb_sample_stats sst;
@@ -986,8 +1087,8 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
     }
     if (stt != TCHEM_GB_SAMPLE_NEGATIVE_DT) {
       double* out = P.state_out + static_cast<size_t>(smp) * P.state_dim;
-      for (int i = lane; i < P.state_dim - 3 - m; i += 32) out[3 + m + i] = row[3 + m + i];
-      if (lane == 0) {
+      for (int i = tid; i < P.state_dim - 3 - m; i += NT) out[3 + m + i] = row[3 + m + i];
+      if (tid == 0) {
         const double rho = row[0];
         out[0] = rho;
         out[1] = p;
@@ -1001,7 +1102,7 @@ __global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_const
         if (i < m) out[3 + i] = y[s];
       }
     }
-    __syncwarp();
+    S.gsync();
   }
 }
 

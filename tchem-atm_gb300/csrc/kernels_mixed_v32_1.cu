@@ -5,7 +5,7 @@
 namespace tchem_gb {
 
 cudaError_t launch_mixed_32_1(const AdvanceParams& P, int grid, int threads, size_t smem, cudaStream_t stream) {
-  auto k = mixed::trbdf2_mixed_kernel<32, 1, false>;
+  auto k = mixed::trbdf2_mixed_kernel<32, 1, false, 1>;
   cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
   if (e != cudaSuccess) return e;
   k<<<grid, threads, smem, stream>>>(P);
@@ -13,7 +13,7 @@ cudaError_t launch_mixed_32_1(const AdvanceParams& P, int grid, int threads, siz
 }
 
 const void* kernel_mixed_32_1() {
-  return reinterpret_cast<const void*>(mixed::trbdf2_mixed_kernel<32, 1, false>);
+  return reinterpret_cast<const void*>(mixed::trbdf2_mixed_kernel<32, 1, false, 1>);
 }
 
 }  // namespace tchem_gb

@@ -1,0 +1,20 @@
+// Instantiation of the simplified-Newton (Gauss-Jordan inverse) mixed-precision kernel with one
+// sample per 4 warps: MC=128 columns, one row per thread (one translation unit per kernel so the
+// kernels compile in parallel).
+#include "kernels_mixed_impl.cuh"
+
+namespace tchem_gb {
+
+cudaError_t launch_simpl_128_1_g4(const AdvanceParams& P, int grid, int threads, size_t smem, cudaStream_t stream) {
+  auto k = mixed::trbdf2_mixed_kernel<128, 1, true, 4>;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+  if (e != cudaSuccess) return e;
+  k<<<grid, threads, smem, stream>>>(P);
+  return cudaGetLastError();
+}
+
+const void* kernel_simpl_128_1_g4() {
+  return reinterpret_cast<const void*>(mixed::trbdf2_mixed_kernel<128, 1, true, 4>);
+}
+
+}  // namespace tchem_gb

@@ -28,6 +28,9 @@ struct tchem_gb_mech {
   std::unique_ptr<tchem_gb::HostTables> host_tables;
   std::vector<tchem_gb::DeviceTables*> device_tables;
   std::mutex mu;
+  // Threads per sample used when a call leaves it to the library (opts.threads_per_sample == 0),
+  // per tchem_gb_form; 0: the narrowest kernel shape. Set by tchem_gb_autotune.
+  int tps_pref[3] = {0, 0, 0};
 
   void build_view();
   ~tchem_gb_mech();

@@ -93,6 +93,9 @@ def lib() -> C.CDLL:
         "tchem_gb_time_advance_record": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                                    C.c_int, vp]),
         "tchem_gb_adjoint_workspace_bytes": (C.c_size_t, [vp, C.c_int]),
+        "tchem_gb_autotune": (C.c_int, [vp, C.c_int, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, C.c_size_t, vp,
+                                        C.POINTER(C.c_int), C.POINTER(C.c_float)]),
+        "tchem_gb_mech_set_threads_per_sample": (C.c_int, [vp, C.c_int, C.c_int]),
         "tchem_gb_adjoint": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp,
                                        C.c_size_t, vp]),
     }

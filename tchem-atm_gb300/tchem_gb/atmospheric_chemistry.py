@@ -148,6 +148,68 @@ class AtmosphericChemistry:
         return state_out, t_o, dt_o, status, stats
 
     @staticmethod
+    def autotune(kmcd: KineticModel, tol_newton, tol_time, tadv, state, *, form: str | int = "simplified",
+                 stream=None):
+        """Times the form's kernel shapes (32/64/128 threads per sample) on the probe batch (device
+        arrays as for runDeviceBatch; the probe starts at t = 0), keeps the fastest as the mechanism's
+        default and returns (threads_per_sample, {shape: ms})."""
+        torch = _torch()
+        B = int(state.shape[0])
+        out = torch.empty_like(state)
+        t = torch.zeros(B, dtype=torch.float64, device=state.device)
+        dt = torch.zeros_like(t)
+        st = torch.empty(B, dtype=torch.int32, device=state.device)
+        chosen = C.c_int(0)
+        ms = (C.c_float * 3)()
+        o = _opts(form)
+        rc = _capi.lib().tchem_gb_autotune(kmcd.handle, o.form, B, _ptr(tol_newton), _ptr(tol_time), _ptr(tadv),
+                                           _ptr(state), _ptr(t), _ptr(dt), _ptr(out), _ptr(st), None, 0,
+                                           _stream_ptr(stream), C.byref(chosen), ms)
+        _capi.check(rc, "tchem_gb_autotune")
+        return chosen.value, {32 * (1 << i): ms[i] for i in range(3) if ms[i] >= 0}
+
+    @staticmethod
+    def set_threads_per_sample(kmcd: KineticModel, threads_per_sample: int, form: str | int = "simplified"):
+        o = _opts(form)
+        _capi.check(_capi.lib().tchem_gb_mech_set_threads_per_sample(kmcd.handle, o.form, int(threads_per_sample)),
+                    "tchem_gb_mech_set_threads_per_sample")
+
+    @staticmethod
+    def capture(tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, kmcd, *, mech_of_sample=None,
+                status=None, form: str | int = "simplified", threads_per_sample: int = 0):
+        """Captures one whole-batch advance -- t_out reset to tadv.tbeg's start (0), the per-sample
+        mechanism bucketing and one persistent kernel per mechanism structure -- into a CUDA graph and
+        returns it; graph.replay() re-runs the batch from its initial state with one launch. The
+        workspace is allocated here, before capture, and kept with the graph."""
+        torch = _torch()
+        mechs = _mechs(kmcd)
+        B = int(state.shape[0])
+        if status is None:
+            status = torch.empty(B, dtype=torch.int32, device=state.device)
+        o = _opts(form, threads_per_sample)
+        n = _capi.lib().tchem_gb_workspace_bytes(_handles(mechs), len(mechs), B, C.byref(o))
+        if n == 0:
+            _capi.check(1, "tchem_gb_workspace_bytes")
+        ws = torch.empty(int(n), dtype=torch.uint8, device=state.device)
+        side = torch.cuda.Stream(device=state.device)
+        side.wait_stream(torch.cuda.current_stream(state.device))
+        with torch.cuda.stream(side):  # one eager run: mechanism tables on the device, kernel attributes set
+            t_out.zero_()
+            AtmosphericChemistry.runDeviceBatch(tol_newton, tol_time, None, tadv, state, t_out, dt_out, state_out,
+                                                kmcd, mech_of_sample=mech_of_sample, status=status, form=form,
+                                                threads_per_sample=threads_per_sample, workspace=ws, stream=side)
+        torch.cuda.current_stream(state.device).wait_stream(side)
+        torch.cuda.synchronize(state.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, capture_error_mode="relaxed"):
+            t_out.zero_()
+            AtmosphericChemistry.runDeviceBatch(tol_newton, tol_time, None, tadv, state, t_out, dt_out, state_out,
+                                                kmcd, mech_of_sample=mech_of_sample, status=status, form=form,
+                                                threads_per_sample=threads_per_sample, workspace=ws)
+        g._tchem_workspace = ws  # keep the workspace alive with the graph
+        return g, status
+
+    @staticmethod
     def device_error(workspace=None, stream=None) -> int:
         err = C.c_int32(0)
         _capi.check(_capi.lib().tchem_gb_device_error(_ptr(workspace), _stream_ptr(stream), C.byref(err)),
