@@ -73,6 +73,10 @@ def parse() -> argparse.Namespace:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--other-samples", type=int, default=65536,
                     help="subsample for the other mixed form (mixed <-> simplified)")
+    ap.add_argument("--uneven-samples", type=int, default=0,
+                    help="samples of the uneven-batch leg (262144 in the reference's uneven configuration): 75 %% on "
+                         "the 51-species and 25 %% on a 120-species mechanism, half night, horizons 600/1800/3600 s, "
+                         "autotuned shapes, one CUDA-graph launch; 0 skips it")
     ap.add_argument("--adjoint-samples", type=int, default=8192,
                     help="samples of the discrete-adjoint leg (1800 s horizon, FP64); 0 skips it")
     return ap.parse_args()
@@ -265,6 +269,67 @@ def reference_arm(args, world: int, rank: int):
     print(json.dumps(line), flush=True)
 
 
+# ---- uneven batch -------------------------------------------------------------------------------
+
+def uneven_leg(B: int, dev, stream) -> dict:
+    """Mixed mechanism sizes, day/night variants and three horizons in one graph-captured launch."""
+    import torch
+    from tchem_gb import AtmosphericChemistry, tadv_to_device
+    spec120 = MechanismSpec(n_species=120, n_reactions=330, seed=20251204)
+    mechs = [KineticModel.from_string(mechanism_yaml(MechanismSpec())),
+             KineticModel.from_string(mechanism_yaml(MechanismSpec(), night=True)),
+             KineticModel.from_string(mechanism_yaml(spec120)),
+             KineticModel.from_string(mechanism_yaml(spec120, night=True))]
+    rng = np.random.default_rng(20251205)
+    big = rng.random(B) < 0.25
+    night = rng.random(B) < 0.5
+    mos = (2 * big + night).astype(np.int32)
+    dim = mechs[2].state_dim
+    state = np.zeros((B, dim))
+    s51 = sample_states(B, mechs[0].n_active, seed=SEED + 11)
+    s120 = sample_states(B, mechs[2].n_active, seed=SEED + 12)
+    state[:, :s51.shape[1]] = s51
+    state[big] = s120[big]
+    horizon = rng.choice([600.0, 1800.0, 3600.0], size=B)
+    tadv = np.zeros(B, dtype=_capi.TIME_ADVANCE_DTYPE)
+    tadv["tbeg"], tadv["tend"], tadv["dt"], tadv["dtmin"], tadv["dtmax"] = 0.0, horizon, 1e-10, 1e-10, horizon
+    tadv["max_num_newton_iterations"] = 20
+    tadv["num_time_iterations_per_interval"] = 1_000_000
+    tadv["jacobian_interval"] = 1
+    tol_time = np.tile([ATOL, RTOL], (mechs[2].n_active, 1))
+    d_tn = torch.tensor(TOL_NEWTON, dtype=torch.float64, device=dev)
+    d_tt = torch.as_tensor(tol_time).to(dev)
+    tuned = {}
+    for k in (0, 2):  # autotune each structure on a probe of its own samples
+        sel = np.nonzero(mos == k)[0][:2048]
+        km = mechs[k]
+        tps, times = AtmosphericChemistry.autotune(km, d_tn, d_tt[:km.n_active], tadv_to_device(tadv[sel], dev),
+                                                   torch.as_tensor(state[sel][:, :km.state_dim]).to(dev),
+                                                   form="simplified", stream=stream)
+        AtmosphericChemistry.set_threads_per_sample(mechs[k + 1], tps)
+        tuned[f"{km.n_active}_species"] = {"threads_per_sample": tps,
+                                           "probe_ms": {str(a): round(b, 1) for a, b in times.items()}}
+    d_state = torch.as_tensor(state).to(dev)
+    out = torch.empty_like(d_state)
+    t = torch.zeros(B, dtype=torch.float64, device=dev)
+    dt = torch.zeros_like(t)
+    g, status = AtmosphericChemistry.capture(d_tn, d_tt, tadv_to_device(tadv, dev), d_state, t, dt, out, mechs,
+                                             mech_of_sample=torch.as_tensor(mos).to(dev), form="simplified")
+    g.replay()  # warm-up replay (the capture helper also ran the batch once eagerly)
+    torch.cuda.synchronize(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    g.replay()
+    e1.record()
+    torch.cuda.synchronize(dev)
+    ms = e0.elapsed_time(e1)
+    return {"samples": B, "value": B / (ms * 1e-3), "unit": "samples/s", "ms": ms,
+            "failed_samples": int((status != 0).sum()),
+            "mix": {"51_species": int((~big).sum()), "120_species": int(big.sum()), "night": int(night.sum())},
+            "launch": "one CUDA graph (t reset, bucketing, one persistent kernel per mechanism structure)",
+            "autotuned": tuned}
+
+
 # ---- discrete adjoint -------------------------------------------------------------------------
 
 def adjoint_leg(km, state, tol_time, n: int, dev, stream) -> dict:
@@ -447,6 +512,9 @@ def engine_arm(args, world: int, rank: int, local: int):
                                           f"over samples on {cores} threads ({el:.1f} s)"}
         line["accuracy_vs_fp64_oracle"] = {"samples": n, "max": float(e.max()), "p99": float(np.percentile(e, 99)),
                                            "floor": ATOL}
+
+    if rank == 0 and args.uneven_samples > 0:
+        line["uneven_batch"] = uneven_leg(args.uneven_samples, dev, stream)
 
     if rank == 0 and args.adjoint_samples > 0:
         line["adjoint"] = adjoint_leg(km, state, tol_time, args.adjoint_samples, dev, stream)
