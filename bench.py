@@ -399,6 +399,14 @@ def engine_arm(args, world: int, rank: int, local: int):
     d_dt = torch.zeros_like(d_t)
     d_status = torch.empty(B, dtype=torch.int32, device=dev)
     d_stats = torch.zeros(B, 8, dtype=torch.int32, device=dev)
+    tuned = None
+    if args.form != "plain":
+        # the autotuner picks the kernel shape (threads per sample) on a probe of the batch
+        P0 = min(4096, B)
+        tps, times = AtmosphericChemistry.autotune(km, d_tn, d_tt, d_tadv[:P0], d_state[:P0].contiguous(),
+                                                   form=args.form, stream=stream)
+        tuned = {"threads_per_sample": tps, "probe_samples": P0,
+                 "probe_ms": {str(a): round(b, 1) for a, b in times.items()}}
     ws_bytes = AtmosphericChemistry.getWorkSpaceSize(km, B, form=args.form)
     d_ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
 
@@ -448,7 +456,7 @@ def engine_arm(args, world: int, rank: int, local: int):
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": FORM_DTYPE[args.form], "data": "synthetic (seeded CB05-shaped mechanism and states)",
-        "config": bench_config(B, args.form, world),
+        "config": {**bench_config(B, args.form, world), "autotuned": tuned},
         "failed_samples": n_fail,
         "work_per_sample": {k: float(stats[:, i].mean()) for i, k in enumerate(
             ["steps", "rejected", "newton_fail", "newton_iter", "factorizations", "solves", "rhs", "jacobians"])},

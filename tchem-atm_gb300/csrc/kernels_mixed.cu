@@ -29,10 +29,9 @@ TCHEM_GB_DECLARE_SHAPE(simpl, 128, 1_g4)
 
 namespace {
 
-constexpr int kMaxWarps = 8;
-
 struct Variant {
   int MC, RPT, G;  // columns, rows per thread, warps per sample
+  int max_warps;   // per CTA (the kernel's launch bounds)
   bool simplified;
   const void* kernel;
   cudaError_t (*launch)(const AdvanceParams&, int, int, size_t, cudaStream_t);
@@ -42,16 +41,16 @@ struct Variant {
 // among those with the requested threads per sample (32 G; 0: any, fewest warps first).
 const Variant* variants(int* n) {
   static const Variant v[] = {
-      {24, 1, 1, false, kernel_mixed_24_1(), &launch_mixed_24_1},
-      {32, 1, 1, false, kernel_mixed_32_1(), &launch_mixed_32_1},
-      {52, 2, 1, false, kernel_mixed_52_2(), &launch_mixed_52_2},
-      {64, 2, 1, false, kernel_mixed_64_2(), &launch_mixed_64_2},
-      {24, 1, 1, true, kernel_simpl_24_1(), &launch_simpl_24_1},
-      {32, 1, 1, true, kernel_simpl_32_1(), &launch_simpl_32_1},
-      {52, 2, 1, true, kernel_simpl_52_2(), &launch_simpl_52_2},
-      {64, 2, 1, true, kernel_simpl_64_2(), &launch_simpl_64_2},
-      {64, 1, 2, true, kernel_simpl_64_1_g2(), &launch_simpl_64_1_g2},
-      {128, 1, 4, true, kernel_simpl_128_1_g4(), &launch_simpl_128_1_g4},
+      {24, 1, 1, 12, false, kernel_mixed_24_1(), &launch_mixed_24_1},
+      {32, 1, 1, 12, false, kernel_mixed_32_1(), &launch_mixed_32_1},
+      {52, 2, 1, 8, false, kernel_mixed_52_2(), &launch_mixed_52_2},
+      {64, 2, 1, 8, false, kernel_mixed_64_2(), &launch_mixed_64_2},
+      {24, 1, 1, 12, true, kernel_simpl_24_1(), &launch_simpl_24_1},
+      {32, 1, 1, 12, true, kernel_simpl_32_1(), &launch_simpl_32_1},
+      {52, 2, 1, 8, true, kernel_simpl_52_2(), &launch_simpl_52_2},
+      {64, 2, 1, 8, true, kernel_simpl_64_2(), &launch_simpl_64_2},
+      {64, 1, 2, 12, true, kernel_simpl_64_1_g2(), &launch_simpl_64_1_g2},
+      {128, 1, 4, 8, true, kernel_simpl_128_1_g4(), &launch_simpl_128_1_g4},
   };
   *n = static_cast<int>(sizeof(v) / sizeof(v[0]));
   return v;
@@ -81,7 +80,7 @@ MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_cou
   const MixedLayout ml = mixed::make_layout(L, best->MC, simplified);
   const size_t gbytes = ml.warp_bytes;
   const size_t avail = static_cast<size_t>(max_smem_optin) - 16 - L.blob_bytes;
-  const int groups = static_cast<int>(std::min<size_t>(kMaxWarps / best->G, avail / gbytes));
+  const int groups = static_cast<int>(std::min<size_t>(best->max_warps / best->G, avail / gbytes));
   if (groups < 1) throw std::domain_error("mixed form: shared-memory working set too large");
   const int warps = groups * best->G;
   MixedConfig mc;

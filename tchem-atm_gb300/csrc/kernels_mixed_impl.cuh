@@ -115,6 +115,14 @@ struct Solver {
       return tid;
     }
   }
+  // first sliced-ELL slice of this warp (slices go round-robin to the group's warps)
+  __device__ __forceinline__ int wslice() const {
+    if constexpr (G == 1) {
+      return 0;
+    } else {
+      return wid;
+    }
+  }
   __device__ __forceinline__ int row(int s) const {
     if constexpr (G == 1) {
       return lane + 32 * s;
@@ -218,7 +226,7 @@ struct Solver {
     const double* wse_nu = t<double>(L.off_wse_nu);
     const double* emis = t<double>(L.off_emis);
 #pragma unroll 2
-    for (int sl = wid; sl < L.NWS; sl += G) {
+    for (int sl = wslice(); sl < L.NWS; sl += G) {
       const int sp = ws_sp[sl * 32 + lane];
       const int cnt = ws_cnt[sl];
       const int base = ws_off[sl] + lane;
@@ -359,7 +367,7 @@ struct Solver {
     const float* jse_nu = t<float>(L.off_jse_nu32);
     // Jacobian nonzeros over slices (sliced ELL): uniform trip counts, independent loads
 #pragma unroll 2
-    for (int sl = wid; sl < L.NJS; sl += G) {
+    for (int sl = wslice(); sl < L.NJS; sl += G) {
       const int rc = js_rc[sl * 32 + lane];
       const int cnt = js_cnt[sl];
       const int base = js_off[sl] + lane;
@@ -566,7 +574,7 @@ struct Solver {
     for (int k = 0; k < mm; ++k) {
       if ((gk & ~KMASK) == 0u || (gk & ~KMASK) >= 0x7f800000u) return false;  // zero column, inf or nan
       const int p = static_cast<int>(KMASK - (gk & KMASK));
-      const int owner = p % NT, pslot = p / NT;
+      const int owner = static_cast<int>(static_cast<unsigned>(p) % NT), pslot = static_cast<int>(static_cast<unsigned>(p) / NT);
       const bool is_owner = gt() == owner;
       float pv_mine = A[0][0];
 #pragma unroll
@@ -809,12 +817,22 @@ struct Solver {
           dbits = max(dbits, __float_as_uint(static_cast<float>(fabs(dx[s]))));
         }
       }
-      const uint32_t flags = gor_u32((finite ? 0u : 1u) | (conv ? 0u : 2u));
-      if (flags & 1u) return false;
-      const float dmax = __uint_as_float(gmax_u32(dbits));
+      bool all_finite, all_conv;
+      float dmax;
+      if constexpr (G == 1) {
+        all_finite = __all_sync(kFullMask, finite);
+        dmax = __uint_as_float(__reduce_max_sync(kFullMask, dbits));
+        all_conv = __all_sync(kFullMask, conv);
+      } else {
+        const uint32_t flags = gor_u32((finite ? 0u : 1u) | (conv ? 0u : 2u));
+        all_finite = !(flags & 1u);
+        all_conv = !(flags & 2u);
+        dmax = __uint_as_float(gmax_u32(dbits));
+      }
+      if (!all_finite) return false;
       if (it > 0 && !fresh && dmax > 0.5f * prev) refresh = true;
       prev = dmax;
-      if (!(flags & 2u)) return true;
+      if (all_conv) return true;
     }
     return false;
   }
@@ -991,8 +1009,16 @@ struct Solver {
 
 // One sample per group of G warps (G = 1: one warp), persistent work queue (same outer protocol as
 // the plain kernel).
+// Shapes with one row per thread hold half the matrix registers of the two-rows-per-lane shapes,
+// so they fit 168 registers and run 12 warps per SM; the others run 8.
 template <int MC, int RPT, bool SIMP, int G>
-__global__ void __launch_bounds__(256, 1) trbdf2_mixed_kernel(const __grid_constant__ AdvanceParams P) {
+constexpr int max_threads() {
+  return (RPT == 1 && MC <= 64) ? 384 : 256;
+}
+
+template <int MC, int RPT, bool SIMP, int G>
+__global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G>(), 1)
+    trbdf2_mixed_kernel(const __grid_constant__ AdvanceParams P) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
   unsigned char* tables = smem + 16;
