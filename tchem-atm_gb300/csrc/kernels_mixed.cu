@@ -23,6 +23,7 @@ TCHEM_GB_DECLARE_SHAPE(simpl, 24, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 32, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 52, 2)
 TCHEM_GB_DECLARE_SHAPE(simpl, 64, 2)
+TCHEM_GB_DECLARE_SHAPE(simpl, 52, 1_g2)
 TCHEM_GB_DECLARE_SHAPE(simpl, 64, 1_g2)
 TCHEM_GB_DECLARE_SHAPE(simpl, 128, 1_g4)
 #undef TCHEM_GB_DECLARE_SHAPE
@@ -49,6 +50,7 @@ const Variant* variants(int* n) {
       {32, 1, 1, 12, true, kernel_simpl_32_1(), &launch_simpl_32_1},
       {52, 2, 1, 8, true, kernel_simpl_52_2(), &launch_simpl_52_2},
       {64, 2, 1, 8, true, kernel_simpl_64_2(), &launch_simpl_64_2},
+      {52, 1, 2, 16, true, kernel_simpl_52_1_g2(), &launch_simpl_52_1_g2},
       {64, 1, 2, 12, true, kernel_simpl_64_1_g2(), &launch_simpl_64_1_g2},
       {128, 1, 4, 8, true, kernel_simpl_128_1_g4(), &launch_simpl_128_1_g4},
   };

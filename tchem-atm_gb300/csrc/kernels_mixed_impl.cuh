@@ -1010,10 +1010,11 @@ struct Solver {
 // One sample per group of G warps (G = 1: one warp), persistent work queue (same outer protocol as
 // the plain kernel).
 // Shapes with one row per thread hold half the matrix registers of the two-rows-per-lane shapes,
-// so they fit 168 registers and run 12 warps per SM; the others run 8.
+// so they fit 168 registers and run 12 warps per SM (the 52-column two-warp shape 128 registers
+// and 16 warps); the others run 8.
 template <int MC, int RPT, bool SIMP, int G>
 constexpr int max_threads() {
-  return (RPT == 1 && MC <= 64) ? 384 : 256;
+  return (RPT == 1 && MC <= 52 && G == 2) ? 512 : ((RPT == 1 && MC <= 64) ? 384 : 256);
 }
 
 template <int MC, int RPT, bool SIMP, int G>
