@@ -185,7 +185,9 @@ def dist_setup(n_gpus: int):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group(backend="nccl" if n_gpus > 0 else "gloo")
+        import torch
+        # one GPU per rank over NCCL; gloo where there is no GPU (the CPU-only reference arm)
+        dist.init_process_group(backend="nccl" if n_gpus > 0 and torch.cuda.is_available() else "gloo")
     return world, rank, local
 
 
