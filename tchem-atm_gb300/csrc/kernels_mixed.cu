@@ -19,6 +19,7 @@ TCHEM_GB_DECLARE_SHAPE(mixed, 24, 1)
 TCHEM_GB_DECLARE_SHAPE(mixed, 32, 1)
 TCHEM_GB_DECLARE_SHAPE(mixed, 52, 2)
 TCHEM_GB_DECLARE_SHAPE(mixed, 64, 2)
+TCHEM_GB_DECLARE_SHAPE(mixed, 52, 1_g2)
 TCHEM_GB_DECLARE_SHAPE(simpl, 24, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 32, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 52, 2)
@@ -46,6 +47,7 @@ const Variant* variants(int* n) {
       {32, 1, 1, 12, false, kernel_mixed_32_1(), &launch_mixed_32_1},
       {52, 2, 1, 8, false, kernel_mixed_52_2(), &launch_mixed_52_2},
       {64, 2, 1, 8, false, kernel_mixed_64_2(), &launch_mixed_64_2},
+      {52, 1, 2, 16, false, kernel_mixed_52_1_g2(), &launch_mixed_52_1_g2},
       {24, 1, 1, 12, true, kernel_simpl_24_1(), &launch_simpl_24_1},
       {32, 1, 1, 12, true, kernel_simpl_32_1(), &launch_simpl_32_1},
       {52, 2, 1, 8, true, kernel_simpl_52_2(), &launch_simpl_52_2},

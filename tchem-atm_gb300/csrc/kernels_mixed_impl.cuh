@@ -83,7 +83,7 @@ inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified) {
 template <int MC, int RPT, bool SIMP, int G = 1>
 struct Solver {
   static_assert(MC % 4 == 0, "MC must be a multiple of 4");
-  static_assert(G == 1 || (SIMP && RPT == 1), "multi-warp samples: simplified form, one row per thread");
+  static_assert(G == 1 || RPT == 1, "multi-warp samples: one row per thread");
   static constexpr int LDU = ldu_for(MC);
   static constexpr int NT = 32 * G;                       // threads per sample
   static constexpr int NROWS = NT * RPT;                  // rows held in registers
@@ -179,6 +179,21 @@ struct Solver {
       return o;
     }
   }
+  __device__ __forceinline__ double gsum_f64(double v) {
+    v = warp_sum(v);
+    if constexpr (G == 1) {
+      return v;
+    } else {
+      double* r = reinterpret_cast<double*>(w<unsigned char>(P.ml.red) + 64) + 8 * rp;
+      rp ^= 1;
+      if (lane == 0) r[wid] = v;
+      gsync();
+      double t = r[0];
+#pragma unroll
+      for (int i = 1; i < G; ++i) t += r[i];
+      return t;
+    }
+  }
   __device__ __forceinline__ double gmax_f64(double v) {
     v = warp_max(v);
     if constexpr (G == 1) {
@@ -255,7 +270,6 @@ struct Solver {
   // dq_r/dx . v = keff_r sum_f v[sp_f] prod_{g != f} x[sp_g], then the net-production program
   // without emissions.
   __device__ __forceinline__ void jvec(const double (&v)[RPT], double (&out)[RPT]) {
-    static_assert(G == 1, "FP32-LU form: one warp per sample");
     const MechLayout& L = P.mech.L;
     double* x = w<double>(P.ml.x);
     double* vv = &vec(V_YP, 0);
@@ -267,10 +281,10 @@ struct Solver {
         x[row(s)] = vec(V_YGP, row(s));
         vv[row(s)] = v[s];
       }
-    __syncwarp();
+    gsync();
     const int32_t* rf_ptr = t<int32_t>(L.off_rf_ptr);
     const int16_t* rf_sp = t<int16_t>(L.off_rf_sp);
-    for (int r = lane; r < L.R; r += 32) {
+    for (int r = gt(); r < L.R; r += NT) {
       const int g0 = rf_ptr[r], g1 = rf_ptr[r + 1];
       double dq = 0.0;
       if (g1 - g0 == 1) {
@@ -288,13 +302,13 @@ struct Solver {
       }
       q[r] = keff[r] * dq;
     }
-    __syncwarp();
+    gsync();
     const int32_t* ws_sp = t<int32_t>(L.off_ws_sp);
     const int32_t* ws_cnt = t<int32_t>(L.off_ws_cnt);
     const int32_t* ws_off = t<int32_t>(L.off_ws_off);
     const int16_t* wse_r = t<int16_t>(L.off_wse_r);
     const double* wse_nu = t<double>(L.off_wse_nu);
-    for (int sl = 0; sl < L.NWS; ++sl) {
+    for (int sl = wslice(); sl < L.NWS; sl += G) {
       const int sp = ws_sp[sl * 32 + lane];
       const int cnt = ws_cnt[sl];
       const int base = ws_off[sl] + lane;
@@ -308,10 +322,10 @@ struct Solver {
       if (c < cnt) a0 += wse_nu[base + 32 * c] * q[wse_r[base + 32 * c]];
       if (sp >= 0) x[sp] = a0 + a1;
     }
-    __syncwarp();
+    gsync();
 #pragma unroll
     for (int s = 0; s < RPT; ++s) out[s] = row(s) < L.m ? x[row(s)] : 0.0;
-    __syncwarp();
+    gsync();
     count(S_RHS);
   }
 
@@ -474,8 +488,6 @@ struct Solver {
   // the next step's pivot reduction is issued as soon as the first column group is updated, so
   // its latency overlaps the rest of the update.
   __device__ __forceinline__ bool factor_fwd(float (&wf)[RPT]) {
-    static_assert(G == 1, "FP32-LU form: one warp per sample");
-    static_assert(32 * RPT <= 64, "row index must fit the 6 key bits");
     constexpr int NG = MC / 4;
     constexpr int C1 = (NG + 2) / 3, C2 = (2 * NG + 2) / 3;
     const int mm = m();
@@ -491,13 +503,13 @@ struct Solver {
       act[s] = row(s) < mm;
       step[s] = INT_MAX;
     }
-    uint32_t gk = __reduce_max_sync(kFullMask, pivot_key(act));
+    uint32_t gk = gmax_u32(pivot_key(act));
 #pragma unroll 1
     for (int k = 0; k < mm; ++k) {
-      if ((gk >> 6) == 0u || (gk & ~63u) >= 0x7f800000u) return false;  // zero column, inf or nan
-      const int p = 63 - static_cast<int>(gk & 63u);
-      const int owner = p & 31, pslot = p >> 5;
-      const bool is_owner = lane == owner;
+      if ((gk & ~KMASK) == 0u || (gk & ~KMASK) >= 0x7f800000u) return false;  // zero column, inf or nan
+      const int p = static_cast<int>(KMASK - (gk & KMASK));
+      const int owner = static_cast<int>(static_cast<unsigned>(p) % NT), pslot = static_cast<int>(static_cast<unsigned>(p) / NT);
+      const bool is_owner = gt() == owner;
       float pv_mine = A[0][0], w_mine = wf[0];
 #pragma unroll
       for (int s = 1; s < RPT; ++s)
@@ -505,8 +517,20 @@ struct Solver {
       // publish the pivot row's U part (registers 1..MC-1) with predicated stores
       float* urow = ustage + k * LDU;
       publish_row(urow, pslot, is_owner);
-      const float pval = __shfl_sync(kFullMask, pv_mine, owner);
-      const float yk = __shfl_sync(kFullMask, w_mine, owner);
+      float pval, yk;
+      if constexpr (G == 1) {
+        pval = __shfl_sync(kFullMask, pv_mine, owner);
+        yk = __shfl_sync(kFullMask, w_mine, owner);
+      } else {
+        float* pvb = reinterpret_cast<float*>(w<unsigned char>(P.ml.red) + 192) + 2 * (k & 1);
+        if (is_owner) {
+          pvb[0] = pv_mine;
+          pvb[1] = w_mine;
+        }
+        gsync();  // the pivot, its right-hand side and the published row are visible to the group
+        pval = pvb[0];
+        yk = pvb[1];
+      }
       const float pinv = __fdividef(1.f, pval);
       if (is_owner) {
         pinv_s[k] = pinv;
@@ -526,20 +550,21 @@ struct Solver {
           wf[s] = fmaf(-l[s], yk, wf[s]);
         }
       }
-      __syncwarp();
+      if constexpr (G == 1) __syncwarp();
       // first group (holds the next pivot column), then the next step's pivot reduction, then
       // the rest of the update
       const float zero[RPT] = {};
       update_chunk<0, 1>(l, urow, zero);
-      gk = __reduce_max_sync(kFullMask, pivot_key(act));
+      gk = gmax_u32(pivot_key(act));
       const int width = mm - 1 - k;
       update_chunk<1, C1>(l, urow, zero);
       if (4 * C1 < width) {
         update_chunk<C1, C2>(l, urow, zero);
         if (4 * C2 < width) update_chunk<C2, NG>(l, urow, zero);
       }
-      __syncwarp();
+      if constexpr (G == 1) __syncwarp();
     }
+    gsync();  // factors, step-ordered values and pivots visible to the group
     count(S_LU);
     return true;
   }
@@ -674,7 +699,6 @@ struct Solver {
   // Forward substitution with the stored multipliers (rows' values in wf, in place); leaves the
   // values in step order in ybuf.
   __device__ __forceinline__ void forward(float (&wf)[RPT]) {
-    static_assert(G == 1, "FP32-LU form: one warp per sample");
     const int mm = m();
     const float* lrow = w<float>(P.ml.lrow);
     const int* piv = w<int>(P.ml.piv);
@@ -683,11 +707,19 @@ struct Solver {
 #pragma unroll 1
     for (int k = 0; k < mm; ++k) {
       const int p = piv[k];
-      float mine = 0.f;
+      float yk;
+      if constexpr (G == 1) {
+        float mine = 0.f;
 #pragma unroll
-      for (int s = 0; s < RPT; ++s)
-        if ((p >> 5) == s) mine = wf[s];
-      const float yk = __shfl_sync(kFullMask, mine, p & 31);
+        for (int s = 0; s < RPT; ++s)
+          if ((p >> 5) == s) mine = wf[s];
+        yk = __shfl_sync(kFullMask, mine, p & 31);
+      } else {
+        // the pivot row's value is final at its step: its owner writes it where the others read it
+        if (gt() == p % NT) ybuf[k] = wf[0];
+        gsync();
+        yk = ybuf[k];
+      }
 #pragma unroll
       for (int s = 0; s < RPT; ++s)
         if (step[s] > k && row(s) < mm) wf[s] = fmaf(-lrow[row(s) * LDL + k], yk, wf[s]);
@@ -695,7 +727,7 @@ struct Solver {
 #pragma unroll
     for (int s = 0; s < RPT; ++s)
       if (row(s) < mm) ybuf[step[s]] = wf[s];
-    __syncwarp();
+    gsync();
   }
 
   // Back substitution from ybuf (values in step order) to x in species order.
@@ -711,14 +743,22 @@ struct Solver {
       pv[s] = row(s) < mm ? pinv_s[row(s)] : 0.f;
       xs[s] = 0.f;
     }
-    __syncwarp();
+    gsync();
+    float* xb = w<float>(P.ml.ybuf);  // G > 1: x_k by step, for the group (ybuf is read above)
 #pragma unroll 1
     for (int k = mm - 1; k >= 0; --k) {
-      float mine = 0.f;
+      float xk;
+      if constexpr (G == 1) {
+        float mine = 0.f;
 #pragma unroll
-      for (int s = 0; s < RPT; ++s)
-        if ((k >> 5) == s) mine = ys[s] * pv[s];
-      const float xk = __shfl_sync(kFullMask, mine, k & 31);
+        for (int s = 0; s < RPT; ++s)
+          if ((k >> 5) == s) mine = ys[s] * pv[s];
+        xk = __shfl_sync(kFullMask, mine, k & 31);
+      } else {
+        if (gt() == k % NT) xb[k] = ys[0] * pv[0];
+        gsync();
+        xk = xb[k];
+      }
 #pragma unroll
       for (int s = 0; s < RPT; ++s) {
         const int i = row(s);
@@ -728,6 +768,7 @@ struct Solver {
     }
 #pragma unroll
     for (int s = 0; s < RPT; ++s) x[s] = static_cast<double>(xs[s]);
+    gsync();  // ybuf is reused by the next solve
     count(S_SOLVE);
   }
 
@@ -772,7 +813,7 @@ struct Solver {
           sy += y[s] * y[s];
         }
       }
-      const double ndx = sqrt(warp_sum(sdx)), ny = sqrt(warp_sum(sy));
+      const double ndx = sqrt(gsum_f64(sdx)), ny = sqrt(gsum_f64(sy));
       if (!isfinite(ndx) || !isfinite(ny)) return false;
       if (ndx <= atol + rtol * ny) return true;
     }

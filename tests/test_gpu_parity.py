@@ -268,7 +268,7 @@ def test_simplified_form_follows_its_oracle_restatement(cfg1_like):
 
 
 @pytest.mark.parametrize("form", MIXED_FORMS)
-@pytest.mark.parametrize("tps", [0, 32])
+@pytest.mark.parametrize("tps", [0, 32, 64])
 def test_mixed_threads_per_sample_shapes_agree(cb05, tps, form):
     km, state, tadv, tol_time = generated_case(24, seed=31, horizon=600.0, km=cb05)
     ref = Oracle([km]).time_advance(tadv, state, [1e-18, 1e-8], tol_time)
