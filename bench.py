@@ -53,11 +53,12 @@ SEED = 7
 # Form names of the C ABI's tchem_gb_form.
 FORM_DTYPE = {"plain": "f64", "mixed": "f64 state / f32 LU + f64-residual refinement",
               "simplified": "f64 state / f32 Gauss-Jordan inverse"}
-# DRAM bytes per sample of the simplified-form kernel, from one ncu capture of a 4096-sample,
-# 600 s case (profiles/trbdf2_simplified_cb05_4096.md: 2,365,440 bytes read, 0 written -- the
-# results were still in L2 when the capture ended). The per-sample traffic (state, time-advance
-# record and times read once) does not depend on the horizon, so it scales by samples.
-NCU_DRAM_BYTES_PER_SAMPLE = {"simplified": 2365440 / 4096}
+# DRAM bytes per sample of the simplified-form kernel in the autotuned two-warp shape, from one ncu
+# capture of a 4096-sample, 600 s case (profiles/trbdf2_simplified_2warp_cb05_4096.md: 2,656,512
+# bytes read, 0 written -- the results were still in L2 when the capture ended). The per-sample
+# traffic (state, time-advance record and times read once) does not depend on the horizon, so it
+# scales by samples.
+NCU_DRAM_BYTES_PER_SAMPLE = {"simplified": 2656512 / 4096}
 
 
 def parse() -> argparse.Namespace:

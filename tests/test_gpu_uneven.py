@@ -145,3 +145,16 @@ def test_autotune_and_graph_replay_of_an_uneven_batch():
     for i, b in enumerate(pick):
         m = mechs[mos[b]].n_active
         assert rel_error(eager[b, 3:3 + m], ref[0][i, 3:3 + m], ATOL).max() <= 1e-6, b
+
+
+def test_300_species_mechanism_plain_form():
+    """The plain FP64 form takes any mechanism size (its Newton matrix moves to global memory when
+    shared memory cannot hold it): a seeded 300-species / 1000-reaction mechanism, 2 samples over
+    the first millisecond (one warp per sample on a global-memory matrix is slow at this size)."""
+    km = KineticModel.from_string(mechanism_yaml(MechanismSpec(n_species=300, n_reactions=1000, seed=20251206)))
+    state, tadv, tol_time = case(km, 2, 1e-3, seed=47)
+    m = km.n_active
+    ref = Oracle([km]).time_advance(tadv, state, TN, tol_time)
+    out, st, t = run(km, state, tadv, tol_time, "plain")
+    assert np.all(st == 0) and np.all(t == 1e-3) and np.all(ref[3] == 0)
+    assert rel_error(out[:, 3:3 + m], ref[0][:, 3:3 + m], ATOL).max() <= 1e-8
