@@ -470,7 +470,11 @@ def engine_arm(args, world: int, rank: int, local: int):
                      "peak_source": "FMA-chain probe measured in this run (tchem_gb_measure_fma_peak); "
                                     "MEASURED_PEAKS.json has no FP64/FP32 figure",
                      "fp32": {"achieved": ach32, "peak": peak32.value / 1e12,
-                              "frac": ach32 / (peak32.value / 1e12)}},
+                              "frac": ach32 / (peak32.value / 1e12)},
+                     "note": "algorithmic FP64 flops count the right-hand sides only (the work formula); the FP64 "
+                             "pipe is 61 % busy in ncu for the two-warp simplified kernel "
+                             "(profiles/trbdf2_simplified_2warp_cb05_4096.md): residuals, updates, conversions "
+                             "and step control add to it; the kernel is latency-bound (issue 45 %)"},
     }
 
     if rank == 0:
