@@ -502,6 +502,9 @@ def engine_arm(args, world: int, rank: int, local: int):
             other = "mixed" if args.form == "simplified" else "simplified"
             Q = min(args.other_samples, B)
             if Q > 0 and args.form != "plain":
+                tps_o, _ = AtmosphericChemistry.autotune(km, d_tn, d_tt, d_tadv[:min(4096, Q)],
+                                                         d_state[:min(4096, Q)].contiguous(), form=other,
+                                                         stream=stream)
                 q_out = torch.empty(Q, d_state.shape[1], dtype=torch.float64, device=dev)
                 q_t = torch.zeros(Q, dtype=torch.float64, device=dev)
                 q_dt = torch.zeros_like(q_t)
@@ -512,7 +515,7 @@ def engine_arm(args, world: int, rank: int, local: int):
                 torch.cuda.synchronize(dev)
                 eq = rel_err(q_out[:P].cpu().numpy()[:, 3:3 + m], p_out.cpu().numpy()[:, 3:3 + m])
                 line[f"form_{other}"] = {"value": Q / (ev0.elapsed_time(ev1) * 1e-3), "unit": "samples/s",
-                                         "samples": Q, "dtype": FORM_DTYPE[other],
+                                         "samples": Q, "dtype": FORM_DTYPE[other], "threads_per_sample": tps_o,
                                          "failed_samples": int((st_q != 0).sum()),
                                          "accuracy_vs_plain_fp64_gpu": {"samples": P, "max": float(eq.max()),
                                                                         "p99": float(np.percentile(eq, 99)),

@@ -18,7 +18,7 @@ struct MixedLayout {
   uint32_t warp_bytes;
   uint32_t x, keff, q, x32, keff32, d32, ustage, lrow, pinv, piv, ybuf, vec, stats, red, item;
   int32_t LDU, LDL;
-  int32_t simplified;  // 1: simplified-Newton form (Gauss-Jordan inverse, no L factor region)
+  int32_t simplified;  // 1: simplified-Newton form; 2: full Newton on the Gauss-Jordan inverse; 0: LU
 };
 
 struct AdvanceParams {

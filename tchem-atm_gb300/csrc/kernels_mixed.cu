@@ -19,7 +19,7 @@ TCHEM_GB_DECLARE_SHAPE(mixed, 24, 1)
 TCHEM_GB_DECLARE_SHAPE(mixed, 32, 1)
 TCHEM_GB_DECLARE_SHAPE(mixed, 52, 2)
 TCHEM_GB_DECLARE_SHAPE(mixed, 64, 2)
-TCHEM_GB_DECLARE_SHAPE(mixed, 52, 1_g2)
+TCHEM_GB_DECLARE_SHAPE(mixgj, 52, 1_g2)
 TCHEM_GB_DECLARE_SHAPE(simpl, 24, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 32, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 52, 2)
@@ -34,7 +34,8 @@ namespace {
 struct Variant {
   int MC, RPT, G;  // columns, rows per thread, warps per sample
   int max_warps;   // per CTA (the kernel's launch bounds)
-  bool simplified;
+  bool simplified;  // the form: TCHEM_GB_FORM_MIXED_SIMPLIFIED (else TCHEM_GB_FORM_MIXED)
+  bool gj;          // Gauss-Jordan inverse (else LU)
   const void* kernel;
   cudaError_t (*launch)(const AdvanceParams&, int, int, size_t, cudaStream_t);
 };
@@ -43,18 +44,18 @@ struct Variant {
 // among those with the requested threads per sample (32 G; 0: any, fewest warps first).
 const Variant* variants(int* n) {
   static const Variant v[] = {
-      {24, 1, 1, 12, false, kernel_mixed_24_1(), &launch_mixed_24_1},
-      {32, 1, 1, 12, false, kernel_mixed_32_1(), &launch_mixed_32_1},
-      {52, 2, 1, 8, false, kernel_mixed_52_2(), &launch_mixed_52_2},
-      {64, 2, 1, 8, false, kernel_mixed_64_2(), &launch_mixed_64_2},
-      {52, 1, 2, 16, false, kernel_mixed_52_1_g2(), &launch_mixed_52_1_g2},
-      {24, 1, 1, 12, true, kernel_simpl_24_1(), &launch_simpl_24_1},
-      {32, 1, 1, 12, true, kernel_simpl_32_1(), &launch_simpl_32_1},
-      {52, 2, 1, 8, true, kernel_simpl_52_2(), &launch_simpl_52_2},
-      {64, 2, 1, 8, true, kernel_simpl_64_2(), &launch_simpl_64_2},
-      {52, 1, 2, 16, true, kernel_simpl_52_1_g2(), &launch_simpl_52_1_g2},
-      {64, 1, 2, 12, true, kernel_simpl_64_1_g2(), &launch_simpl_64_1_g2},
-      {128, 1, 4, 8, true, kernel_simpl_128_1_g4(), &launch_simpl_128_1_g4},
+      {24, 1, 1, 12, false, false, kernel_mixed_24_1(), &launch_mixed_24_1},
+      {32, 1, 1, 12, false, false, kernel_mixed_32_1(), &launch_mixed_32_1},
+      {52, 2, 1, 8, false, false, kernel_mixed_52_2(), &launch_mixed_52_2},
+      {64, 2, 1, 8, false, false, kernel_mixed_64_2(), &launch_mixed_64_2},
+      {52, 1, 2, 16, false, true, kernel_mixgj_52_1_g2(), &launch_mixgj_52_1_g2},
+      {24, 1, 1, 12, true, true, kernel_simpl_24_1(), &launch_simpl_24_1},
+      {32, 1, 1, 12, true, true, kernel_simpl_32_1(), &launch_simpl_32_1},
+      {52, 2, 1, 8, true, true, kernel_simpl_52_2(), &launch_simpl_52_2},
+      {64, 2, 1, 8, true, true, kernel_simpl_64_2(), &launch_simpl_64_2},
+      {52, 1, 2, 16, true, true, kernel_simpl_52_1_g2(), &launch_simpl_52_1_g2},
+      {64, 1, 2, 12, true, true, kernel_simpl_64_1_g2(), &launch_simpl_64_1_g2},
+      {128, 1, 4, 8, true, true, kernel_simpl_128_1_g4(), &launch_simpl_128_1_g4},
   };
   *n = static_cast<int>(sizeof(v) / sizeof(v[0]));
   return v;
@@ -81,7 +82,8 @@ MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_cou
     throw std::domain_error(simplified ? "simplified form: no kernel shape for this mechanism size and threads_per_sample "
                                          "(up to 64 species with 32 or 64 threads, 128 with 128 threads)"
                                        : "FP32-LU form: mechanisms with more than 64 active species are not supported");
-  const MixedLayout ml = mixed::make_layout(L, best->MC, simplified);
+  MixedLayout ml = mixed::make_layout(L, best->MC, best->gj);
+  ml.simplified = simplified ? 1 : (best->gj ? 2 : 0);
   const size_t gbytes = ml.warp_bytes;
   const size_t avail = static_cast<size_t>(max_smem_optin) - 16 - L.blob_bytes;
   const int groups = static_cast<int>(std::min<size_t>(best->max_warps / best->G, avail / gbytes));
@@ -104,7 +106,7 @@ MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_cou
 
 cudaError_t launch_trbdf2_mixed(const AdvanceParams& P, const MechLayout& L, int grid, int warps_per_block,
                                 size_t smem, int threads_per_sample, cudaStream_t stream) {
-  const Variant* best = pick(L, P.ml.simplified != 0, threads_per_sample);
+  const Variant* best = pick(L, P.ml.simplified == 1, threads_per_sample);
   if (!best) return cudaErrorInvalidValue;
   return best->launch(P, grid, warps_per_block * 32, smem, stream);
 }

@@ -80,8 +80,15 @@ inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified) {
 // loops stride over the group's 32 G threads, the sliced-ELL programs go slice by slice to the
 // group's warps, and reductions and the pivot broadcast go through shared memory with a named
 // barrier per group.
-template <int MC, int RPT, bool SIMP, int G = 1>
+//
+// FULLGJ (with SIMP) keeps the Gauss-Jordan linear algebra but runs the reference's full Newton
+// (a new matrix every jacobian_interval iterations, the reference's stage guesses and 2-norm
+// test) with one FP64-residual refinement sweep per solve, like the FP32-LU form: it follows the
+// FP64 Newton iterates with matrix-vector solves instead of triangular ones.
+template <int MC, int RPT, bool SIMP, int G = 1, bool FULLGJ = false>
 struct Solver {
+  static_assert(!FULLGJ || SIMP, "the full-Newton Gauss-Jordan variant uses the inverse");
+  static constexpr bool kSimplifiedNewton = SIMP && !FULLGJ;
   static_assert(MC % 4 == 0, "MC must be a multiple of 4");
   static_assert(G == 1 || RPT == 1, "multi-warp samples: one row per thread");
   static constexpr int LDU = ldu_for(MC);
@@ -878,6 +885,47 @@ struct Solver {
     return false;
   }
 
+  // ---- full Newton with the Gauss-Jordan inverse and one refinement sweep per solve --------
+  __device__ __forceinline__ bool newton_full_gj(double (&y)[RPT], const double (&rv)[RPT], double coef,
+                                                 int max_newton, int jac_interval, double atol, double rtol) {
+    for (int it = 0; it < max_newton; ++it) {
+      double f[RPT], dx[RPT], g[RPT], jd[RPT], corr[RPT];
+      float wf[RPT];
+      rhs(y, f);
+#pragma unroll
+      for (int s = 0; s < RPT; ++s) {
+        g[s] = -((y[s] - coef * f[s]) - rv[s]);
+        wf[s] = static_cast<float>(g[s]);
+      }
+      if (it % jac_interval == 0) {
+        newton_matrix(y, coef);
+        put(V_YGP, y);  // the point of the inverted Jacobian, for the refinement residual
+        if (!invert()) return false;
+      }
+      apply_inverse(wf, dx);
+      // refinement: FP64 residual of (I - c J) dx = g, correction through the FP32 inverse
+      jvec(dx, jd);
+#pragma unroll
+      for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(g[s] - (dx[s] - coef * jd[s]));
+      apply_inverse(wf, corr);
+      count(S_NEWTON);
+      double sdx = 0.0, sy = 0.0;
+#pragma unroll
+      for (int s = 0; s < RPT; ++s) {
+        if (row(s) < m()) {
+          dx[s] += corr[s];
+          y[s] += dx[s];
+          sdx += dx[s] * dx[s];
+          sy += y[s] * y[s];
+        }
+      }
+      const double ndx = sqrt(gsum_f64(sdx)), ny = sqrt(gsum_f64(sy));
+      if (!isfinite(ndx) || !isfinite(ny)) return false;
+      if (ndx <= atol + rtol * ny) return true;
+    }
+    return false;
+  }
+
   // Stores a row-distributed vector into the shared stage-vector slot v.
   __device__ __forceinline__ void put(int v, const double (&a)[RPT]) const {
 #pragma unroll
@@ -915,7 +963,7 @@ struct Solver {
         if (last) dt = t_end - t;
         if (!(dt > 0.0)) { status = TCHEM_GB_SAMPLE_DT_UNDERFLOW; break; }
         const double coef = d * dt;
-        if constexpr (SIMP) {
+        if constexpr (kSimplifiedNewton) {
           // keep the carried inverse while c moved by at most 30%
           if (!(have_inv && fabs(coef / c_inv - 1.0) <= 0.3)) have_inv = false;
         }
@@ -930,7 +978,7 @@ struct Solver {
             rv[s] = stage == 0 ? y[s] + coef * vec(V_FN, i) : cg * yg[s] - cn * y[s];
             guess[s] = stage == 0 ? y[s] : yg[s];
           }
-          if constexpr (SIMP) {
+          if constexpr (kSimplifiedNewton) {
             if (stage == 0 && have_prev) {
               // stage-1 guess: the quadratic through the last step's y_{n-1}, y_{n-1+gamma}, y_n
               const double t0 = -dtp, t1 = -(1.0 - gamma) * dtp, tt = gamma * dt;
@@ -953,6 +1001,8 @@ struct Solver {
             }
             fresh = false;
             ok = newton_simplified(guess, rv, coef, max_newton, natol_c, nrtol);
+          } else if constexpr (SIMP) {
+            ok = newton_full_gj(guess, rv, coef, max_newton, jac_interval, natol, nrtol);
           } else {
             ok = newton(guess, rv, coef, max_newton, jac_interval, natol, nrtol);
           }
@@ -987,7 +1037,10 @@ struct Solver {
         float wf[RPT];
 #pragma unroll
         for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(est[s]);
-        if constexpr (SIMP) {
+        if constexpr (FULLGJ) {
+          // filter with the last Newton iteration's inverse (the reference's matrix)
+          apply_inverse(wf, estf);
+        } else if constexpr (SIMP) {
           // filter with I - c J(y_{n+1}); the inverse is carried into the next step
           newton_matrix(y1, d * dt);
           if (invert()) {
@@ -1016,7 +1069,7 @@ struct Solver {
       if (!isfinite(err)) { status = TCHEM_GB_SAMPLE_NONFINITE; break; }
       if (err <= 1.0 || dt <= dt_min) {
         t = last ? t_end : t + dt;
-        if constexpr (SIMP) {
+        if constexpr (kSimplifiedNewton) {
           put(V_YP, y);
           put(V_YGP, yg);
           dtp = dt;
@@ -1053,13 +1106,13 @@ struct Solver {
 // Shapes with one row per thread hold half the matrix registers of the two-rows-per-lane shapes,
 // so they fit 168 registers and run 12 warps per SM (the 52-column two-warp shape 128 registers
 // and 16 warps); the others run 8.
-template <int MC, int RPT, bool SIMP, int G>
+template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false>
 constexpr int max_threads() {
   return (RPT == 1 && MC <= 52 && G == 2) ? 512 : ((RPT == 1 && MC <= 64) ? 384 : 256);
 }
 
-template <int MC, int RPT, bool SIMP, int G>
-__global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G>(), 1)
+template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false>
+__global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G, FULLGJ>(), 1)
     trbdf2_mixed_kernel(const __grid_constant__ AdvanceParams P) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
@@ -1071,7 +1124,7 @@ __global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G>(), 1)
   }
   constexpr int NT = 32 * G;
   const int group = threadIdx.x / NT, tid = threadIdx.x % NT, lane = threadIdx.x & 31;
-  Solver<MC, RPT, SIMP, G> S{P, tables, tables + L.blob_bytes + group * P.ml.warp_bytes, lane, tid, tid >> 5,
+  Solver<MC, RPT, SIMP, G, FULLGJ> S{P, tables, tables + L.blob_bytes + group * P.ml.warp_bytes, lane, tid, tid >> 5,
                              1 + group};
   const int m = L.m;
   const int n_items = P.n_items_dev ? *P.n_items_dev : P.n_items;

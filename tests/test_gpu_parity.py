@@ -282,7 +282,9 @@ def test_mixed_threads_per_sample_shapes_agree(cb05, tps, form):
     assert int((st != 0).sum()) == 0
     m = km.n_active
     err = rel_error(d_out.cpu().numpy()[:, 3:3 + m], ref[0][:, 3:3 + m], ATOL_TIME)
-    assert err.max() <= 1e-6
+    # every FP32-LU-form shape (LU for one warp, Gauss-Jordan inverse for two) follows the FP64
+    # Newton iterates through its refinement sweep
+    assert err.max() <= (1e-7 if form == "mixed" else 1e-6)
 
 
 @pytest.mark.parametrize("form", MIXED_FORMS)
