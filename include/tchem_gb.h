@@ -132,9 +132,11 @@ int tchem_gb_scenario_read(const char* yaml_path, const tchem_gb_mech* mech, dou
 /* Numerical form of the time advance. */
 enum tchem_gb_form {
   TCHEM_GB_FORM_PLAIN_FP64 = 0, /* FP64 Newton LU: the parity form */
-  /* FP32 Newton LU and solves with one sweep of iterative refinement per Newton solve (FP64
-     residual of the linear system with the FP64 Jacobian, FP32 correction), FP64 Newton
-     residual, state and error control: follows the FP64 form's Newton iterates. */
+  /* The reference's full Newton with FP32 linear algebra -- an LU (one warp per sample) or a
+     Gauss-Jordan inverse (two warps per sample, threads_per_sample = 64) -- and one sweep of
+     iterative refinement per Newton solve (FP64 residual of the linear system with the FP64
+     Jacobian, FP32 correction); FP64 Newton residual, state and error control: follows the FP64
+     form's Newton iterates. */
   TCHEM_GB_FORM_MIXED = 1,
   /* Simplified Newton with an FP32 Gauss-Jordan inverse of I - c J: the inverse is carried from
      the previous step's error filter while c changed by at most 30% (else formed at the first
