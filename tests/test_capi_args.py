@@ -1,0 +1,55 @@
+"""C-ABI argument checking without a GPU: bad arguments come back as TCHEM_GB_ERR_ARG with a
+message, before any device work."""
+from __future__ import annotations
+
+import ctypes as C
+
+from tchem_gb import KineticModel, _capi
+from tchem_gb.generator import MechanismSpec, mechanism_yaml
+
+ERR_ARG = 1
+
+
+def _km():
+    return KineticModel.from_string(mechanism_yaml(MechanismSpec(n_species=20, n_reactions=40, seed=5)))
+
+
+def test_threads_per_sample_preference_is_checked():
+    L = _capi.lib()
+    km = _km()
+    assert L.tchem_gb_mech_set_threads_per_sample(km.handle, 2, 64) == 0
+    assert L.tchem_gb_mech_set_threads_per_sample(km.handle, 2, 0) == 0
+    assert L.tchem_gb_mech_set_threads_per_sample(km.handle, 2, 48) == ERR_ARG
+    assert L.tchem_gb_mech_set_threads_per_sample(km.handle, 7, 32) == ERR_ARG
+    assert L.tchem_gb_mech_set_threads_per_sample(None, 0, 32) == ERR_ARG
+
+
+def test_adjoint_and_record_reject_missing_arrays():
+    L = _capi.lib()
+    km = _km()
+    nul = C.c_void_p(0)
+    rc = L.tchem_gb_adjoint(km.handle, 4, nul, nul, nul, nul, nul, nul, nul, 16, nul, nul, nul, nul, nul, 0, nul)
+    assert rc == ERR_ARG and b"null" in L.tchem_gb_last_error()
+    assert L.tchem_gb_adjoint(km.handle, 0, nul, nul, nul, nul, nul, nul, nul, 16, nul, nul, nul, nul, nul, 0,
+                              nul) == 0  # empty batch
+    rc = L.tchem_gb_time_advance_record(km.handle, 4, nul, nul, nul, nul, nul, nul, nul, nul, nul, nul, nul, nul,
+                                        nul, 0, nul)
+    assert rc == ERR_ARG and b"tape_cap" in L.tchem_gb_last_error()
+
+
+def test_autotune_and_noalloc_reject_bad_arguments():
+    L = _capi.lib()
+    km = _km()
+    nul = C.c_void_p(0)
+    chosen = C.c_int(0)
+    assert L.tchem_gb_autotune(km.handle, 5, 8, nul, nul, nul, nul, nul, nul, nul, nul, nul, 0, nul,
+                               C.byref(chosen), None) == ERR_ARG
+    assert L.tchem_gb_autotune(km.handle, 2, 0, nul, nul, nul, nul, nul, nul, nul, nul, nul, 0, nul,
+                               C.byref(chosen), None) == ERR_ARG
+    f = L.tchem_gb_time_advance_noalloc
+    f.restype = C.c_int
+    f.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_void_p, C.c_int] + [C.c_void_p] * 10 + \
+        [C.POINTER(_capi.AdvanceOpts), C.c_void_p]
+    assert f(None, 1, None, 4, *([None] * 10), None, None) == ERR_ARG
+    handles = (C.c_void_p * 1)(km.handle.value)
+    assert f(handles, 1, None, 0, *([None] * 10), None, None) == 0  # empty batch: nothing to do
