@@ -208,7 +208,7 @@ def max_over_ranks(x: float, world: int, device) -> float:
     return float(t.item())
 
 
-# ---- CPU legs (the oracle is the checker and the CPU restatement) -------------------------------
+# ---- CPU legs (the oracle: accuracy reference and CPU restatement) ------------------------------
 
 def cpu_sample_size(km, state, tadv, tol_time, seconds: float) -> tuple[int, float]:
     """Samples of the CPU oracle that take about `seconds` on all host threads."""

@@ -1,7 +1,7 @@
 /*
  * CPU oracle for the batched box-model TR-BDF2 time advance.
  *
- * TEST INFRASTRUCTURE ONLY. This library is the checker for the GPU engine: it is loaded by
+ * TEST INFRASTRUCTURE ONLY. This library is the GPU engine's accuracy reference: it is loaded by
  * the tests, by the smoke check and by the CPU-baseline leg of bench.py, and by nothing on
  * the product path. It is a plain FP64 C++ restatement of the reference algorithm:
  *   rate constants   src/core/impl/TChem_Impl_KForwardAerosol.hpp:44-145

@@ -10,7 +10,7 @@ Per reaction: 1-2 reactants and 1-4 products with integer stoichiometry. Species
 integer weight and no reaction creates weight, so every mechanism is mass-non-increasing and
 concentrations stay bounded over long horizons.
 
-Rate parameters (BASELINE shape): Arrhenius log10 A ~ U[-16, -10], B ~ U[-3, 3],
+Rate parameters (the benchmark's distributions): Arrhenius log10 A ~ U[-16, -10], B ~ U[-3, 3],
 C ~ U[-2000, 2000] (the reference's form is exp(+C/T); the range is symmetric), D = 300, E = 0;
 Troe with CB05-like falloff parameters; photolysis J log-uniform in [1e-6, 1e-2] s^-1
 (J = 0 for a "night" variant).
