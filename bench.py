@@ -213,7 +213,7 @@ def max_over_ranks(x: float, world: int, device) -> float:
 def cpu_sample_size(km, state, tadv, tol_time, seconds: float) -> tuple[int, float]:
     """Samples of the CPU oracle that take about `seconds` on all host threads."""
     from oracle import Oracle
-    o = Oracle([km])
+    o = Oracle([km], native=True)
     n0 = max(2 * (os.cpu_count() or 1), 16)
     t0 = time.perf_counter()
     o.time_advance(tadv[:n0], state[:n0], TOL_NEWTON, tol_time)
@@ -225,7 +225,7 @@ def cpu_sample_size(km, state, tadv, tol_time, seconds: float) -> tuple[int, flo
 def run_oracle(km, state, tadv, tol_time, n: int):
     from oracle import Oracle
     t0 = time.perf_counter()
-    res = Oracle([km]).time_advance(tadv[:n], state[:n], TOL_NEWTON, tol_time)
+    res = Oracle([km], native=True).time_advance(tadv[:n], state[:n], TOL_NEWTON, tol_time)
     return res, time.perf_counter() - t0
 
 
@@ -256,7 +256,7 @@ def reference_arm(args, world: int, rank: int):
         total += el
     value = n * args.steps / total
     cores = os.cpu_count() or 1
-    sample = (f"first {n} of the {args.samples}-sample CB05-shaped batch per step (FP64 TR-BDF2 CPU restatement, "
+    sample = (f"first {n} of the {args.samples}-sample CB05-shaped batch per step (FP64 TR-BDF2 CPU restatement built for the host CPU, "
               f"OpenMP dynamic over samples on {cores} threads); samples are independent, so box-samples/s "
               f"of the full batch equals this rate")
     line = {
@@ -526,7 +526,7 @@ def engine_arm(args, world: int, rank: int, local: int):
         e = rel_err(out[:n, 3:3 + m], res[0][:, 3:3 + m])
         cores = os.cpu_count() or 1
         line["cpu_baseline"] = {"value": n / el, "unit": "samples/s", "cores": cores, "kind": "port",
-                                "sample": f"first {n} samples of the batch, FP64 TR-BDF2 CPU restatement, OpenMP "
+                                "sample": f"first {n} samples of the batch, FP64 TR-BDF2 CPU restatement built for the host CPU, OpenMP "
                                           f"over samples on {cores} threads ({el:.1f} s)"}
         line["accuracy_vs_fp64_oracle"] = {"samples": n, "max": float(e.max()), "p99": float(np.percentile(e, 99)),
                                            "floor": ATOL}

@@ -6,17 +6,19 @@ from pathlib import Path
 
 import numpy as np
 
-from .build import LIB_PATH, build
+from .build import LIB_PATH, NATIVE_LIB_PATH, build
 
-_lib = None
+_libs: dict = {}
 
 
-def load() -> C.CDLL:
-    global _lib
-    if _lib is None:
-        if not LIB_PATH.exists():
-            build()
-        L = C.CDLL(str(LIB_PATH))
+def load(native: bool = False) -> C.CDLL:
+    """The oracle library: the accuracy reference, or (native) the host-tuned build timed as the
+    CPU baseline."""
+    if native not in _libs:
+        path = NATIVE_LIB_PATH if native else LIB_PATH
+        if not path.exists():
+            build(native=native)
+        L = C.CDLL(str(path))
         vp = C.c_void_p
         L.oracle_kforward.restype = C.c_int
         L.oracle_kforward.argtypes = [vp, C.c_double, C.c_double, vp]
@@ -36,8 +38,8 @@ def load() -> C.CDLL:
         L.oracle_adjoint.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, i]
         L.oracle_tangent.restype = i
         L.oracle_tangent.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, i]
-        _lib = L
-    return _lib
+        _libs[native] = L
+    return _libs[native]
 
 
 def _p(a: np.ndarray | None) -> C.c_void_p:
@@ -51,9 +53,9 @@ class Oracle:
     for the lifetime of this object.
     """
 
-    def __init__(self, models):
+    def __init__(self, models, native: bool = False):
         self.models = list(models)
-        self.lib = load()
+        self.lib = load(native)
         self._views = [m.view for m in self.models]
         self._ptrs = (C.c_void_p * len(self._views))(*[C.cast(C.pointer(v), C.c_void_p) for v in self._views])
 
