@@ -89,6 +89,40 @@ struct AtmosphericChemistry {
           "tchem_gb_time_advance");
   }
 
+  // Autotuner: times the form's kernel shapes on a probe batch (device arrays; t_out is zeroed
+  // before every trial) and keeps the fastest as the mechanism's default; returns its threads
+  // per sample.
+  static int autotune(void* stream, KineticModel& kmcd, int form, int nbatch, const double* tol_newton,
+                      const double* tol_time, const tchem_gb_tadv* tadv, const double* state, double* t_out,
+                      double* dt_out, double* state_out, int32_t* status) {
+    int chosen = 0;
+    check(tchem_gb_autotune(const_cast<tchem_gb_mech*>(kmcd.handle()), form, nbatch, tol_newton, tol_time, tadv,
+                            state, t_out, dt_out, state_out, status, nullptr, 0, stream, &chosen, nullptr),
+          "tchem_gb_autotune");
+    return chosen;
+  }
+
+  // Discrete adjoint (no counterpart in the reference): a plain FP64 run that records its steps,
+  // then dL/dy0 and dL/dtheta (theta_r = log of reaction r's rate-constant scale) from
+  // lambda = dL/dy(t_end). tape_dt [nbatch][tape_cap], tape_ckpt [nbatch][tape_cap/32 + 1][m],
+  // tape_nsteps [nbatch] are caller-owned device arrays.
+  static void recordDeviceBatch(void* stream, const double* tol_newton, const double* tol_time, const double* k_scale,
+                                const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
+                                double* state_out, const KineticModel& kmcd, int nbatch, int32_t* status,
+                                double* tape_dt, double* tape_ckpt, int32_t* tape_nsteps, int tape_cap) {
+    check(tchem_gb_time_advance_record(kmcd.handle(), nbatch, tol_newton, tol_time, k_scale, tadv, state, t_out, dt_out,
+                                       state_out, status, nullptr, tape_dt, tape_ckpt, tape_nsteps, tape_cap, stream),
+          "tchem_gb_time_advance_record");
+  }
+  static void adjointDeviceBatch(void* stream, const double* tol_newton, const double* k_scale,
+                                 const tchem_gb_tadv* tadv, const double* state, const KineticModel& kmcd, int nbatch,
+                                 const double* tape_dt, const double* tape_ckpt, const int32_t* tape_nsteps,
+                                 int tape_cap, const double* lambda, double* grad_x0, double* grad_k, int32_t* status) {
+    check(tchem_gb_adjoint(kmcd.handle(), nbatch, tol_newton, k_scale, tadv, state, tape_dt, tape_ckpt, tape_nsteps,
+                           tape_cap, lambda, grad_x0, grad_k, status, nullptr, 0, stream),
+          "tchem_gb_adjoint");
+  }
+
   // runHostBatch: host arrays, synchronous.
   static void runHostBatch(const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
                            const double* state, double* t_out, double* dt_out, double* state_out,

@@ -182,6 +182,13 @@ def test_cpp_shim_compiles_links_and_parses(tmp_path):
         "  tchem_gb::KineticModel km(argv[1]);\n"
         "  tchem_gb_kmcd_view v = km.view();\n"
         '  std::printf("%d %d %d\\n", v.nSpec, v.nConstSpec, v.nReac);\n'
+        "  if (argc > 2) {  // referenced, not run: the device entry points of the C++ face link\n"
+        "    tchem_gb::AtmosphericChemistry::autotune(nullptr, km, 2, 0, nullptr, nullptr, nullptr, nullptr, nullptr,\n"
+        "                                             nullptr, nullptr, nullptr);\n"
+        "    tchem_gb::AtmosphericChemistry::adjointDeviceBatch(nullptr, nullptr, nullptr, nullptr, nullptr, km, 0,\n"
+        "                                                       nullptr, nullptr, nullptr, 1, nullptr, nullptr, nullptr,\n"
+        "                                                       nullptr);\n"
+        "  }\n"
         "  try { tchem_gb::KineticModel bad(\"/nonexistent.yaml\"); } catch (const std::logic_error&) { return 0; }\n"
         "  return 1;\n}\n")
     exe = tmp_path / "shim"
