@@ -15,7 +15,7 @@
  *                               src/core/TChem_AtmosphericChemistry.cpp:430-508
  *   tchem_gb_workspace_bytes    TChem::AtmosphericChemistry::getWorkSpaceSize
  *                               src/core/TChem_AtmosphericChemistry.hpp:47-81
-  *   tchem_gb_time_advance       TChem::AtmosphericChemistry::runDeviceBatch (both overloads)
+ *   tchem_gb_time_advance       TChem::AtmosphericChemistry::runDeviceBatch (both overloads)
  *                               src/core/TChem_AtmosphericChemistry.hpp:83-155,
  *                               src/core/TChem_AtmosphericChemistry.cpp:211-271, 343-385
  *   tchem_gb_kforward           TChem::Impl::KForwardAerosol::team_invoke
@@ -24,6 +24,17 @@
  *                               src/core/impl/TChem_Impl_ReactionRatesAerosol.hpp:57-143, 238-289
  *   tchem_gb_jacobian           AtmosphericChemistry_Problem::computeJacobian (analytic here)
  *                               src/core/problems/TChem_Impl_AtmosphericChemistry_Problem.hpp:202-213
+ *   tchem_gb_scenario_photolysis_rates, tchem_gb_scenario_external_forcing
+ *                               TChem::AtmChemistry::setScenarioConditionsPhotolysisReactions,
+ *                               setScenarioConditionsExternalForcing
+ *                               src/core/TChem_AtmosphericChemistry.cpp:512-631
+ *   tchem_gb_e3sm_time_advance  TChem::AtmosphericChemistryE3SM::runDeviceBatch
+ *                               src/core/TChem_AtmosphericChemistryE3SM.hpp:88-104
+ *   tchem_gb_e3sm_reaction_rates, _rate_of_progress, _net_production_rates
+ *                               TChem::ReactionRates / RateofProgress / NetProductionRates
+ *                               ::runDeviceBatch, src/core/TChem_ReactionRates.hpp:59-72,
+ *                               src/core/TChem_RateofProgress.hpp:60-75,
+ *                               src/core/TChem_NetProductionRates.hpp:61-78
  */
 #ifndef TCHEM_GB_H
 #define TCHEM_GB_H
@@ -98,6 +109,24 @@ typedef struct tchem_gb_kmcd_view {
   const double* emission_rate;       /* [nEmission] */
 } tchem_gb_kmcd_view;
 
+/* Host view of the E3SM rate tables of a parsed mechanism: the JPL_Coef, R_JPL_ArrheniusCoef,
+ * adjust_reaction and prod_O1D members of TChem::KineticModelNCAR_ConstData
+ * (src/core/TChem_KineticModelNCAR_ConstData.hpp:96-103, types src/core/TChem_Util.hpp:391-459).
+ * Same ownership as tchem_gb_kmcd_view. */
+typedef struct tchem_gb_e3sm_view {
+  int32_t nJPL;
+  const int32_t* jpl_reaction;  /* [nJPL] */
+  const double* jpl_param;      /* [nJPL][7]: k0_A, k0_B, k0_C, kinf_A, kinf_B, kinf_C, Fc */
+  int32_t nRJPL;
+  const int32_t* rjpl_reaction; /* [nRJPL] */
+  const double* rjpl_param;     /* [nRJPL][10]: k0_A, k0_B, k0_C, kinf_A, kinf_B, kinf_C, Fc, A, B, C */
+  int32_t nAdjust;
+  const int32_t* adjust_pair;   /* [nAdjust][2]: reaction, species; applied in this order */
+  int32_t nProdO1D;
+  const int32_t* o1d_index;     /* [nProdO1D][7]: reactions 1..3, photolysis reaction, species 1..3 */
+  const double* o1d_param;      /* [nProdO1D][6]: A1, C1, A2, C2, A3, C3 */
+} tchem_gb_e3sm_view;
+
 /* Per-sample work counters of one time-advance call (the algorithmic-work inputs of the
  * roofline: flops = n_lu*(2/3)m^3 + n_solve*2m^2 + n_jac*F_jac + n_rhs*F_rhs). */
 typedef struct tchem_gb_sample_stats {
@@ -122,12 +151,21 @@ int tchem_gb_mech_create_from_file(const char* yaml_path, const char* echo_path,
 int tchem_gb_mech_create_from_string(const char* yaml_text, tchem_gb_mech** out);
 void tchem_gb_mech_destroy(tchem_gb_mech* mech);
 int tchem_gb_mech_host_view(const tchem_gb_mech* mech, tchem_gb_kmcd_view* view);
+int tchem_gb_mech_e3sm_view(const tchem_gb_mech* mech, tchem_gb_e3sm_view* view);
 /* Copies species name i (truncated as the reference stores it) into buf. */
 int tchem_gb_mech_species_name(const tchem_gb_mech* mech, int i, char* buf, int buflen);
 
 /* Scenario file -> state[nbatch][nSpec+3] on the host ([rho, p, T, x...]). */
 int tchem_gb_scenario_batch_size(const char* yaml_path, int* nbatch);
 int tchem_gb_scenario_read(const char* yaml_path, const tchem_gb_mech* mech, double* state_host, int nbatch);
+/* Scenario file -> photolysis rates photo_host[nbatch][*n_photo] from photolysis_rates.r_0 ..
+ * r_{n_photo-1} (host; *n_photo = 0 without that section; photo_host may be NULL to query
+ * *n_photo). Every list must hold nbatch values. */
+int tchem_gb_scenario_photolysis_rates(const char* yaml_path, int nbatch, double* photo_host, int* n_photo);
+/* Scenario file -> external sources ext_host[nbatch][m] (host; zero where the file's
+ * external_forcing section names no source); *count = the number of forcing entries. */
+int tchem_gb_scenario_external_forcing(const char* yaml_path, const tchem_gb_mech* mech, int nbatch,
+                                       double* ext_host, int* count);
 
 /* Numerical form of the time advance. */
 enum tchem_gb_form {
@@ -265,6 +303,43 @@ int tchem_gb_reaction_rates(const tchem_gb_mech* const* mechs, int n_mechs, cons
                             int nbatch, const double* state, double* omega, void* stream);
 int tchem_gb_jacobian(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
                       const double* state, double* jac, void* stream);
+
+/* ---- E3SM gas chemistry: photolysis rates and external sources as per-sample inputs ---------
+ * TChem::AtmosphericChemistryE3SM::runDeviceBatch (src/core/TChem_AtmosphericChemistryE3SM.hpp:88-104,
+ * src/core/TChem_AtmosphericChemistryE3SM.cpp:42-167) and the RHS-only batch APIs
+ * ReactionRates, RateofProgress and NetProductionRates (src/core/TChem_ReactionRates.hpp:59-72,
+ * src/core/TChem_RateofProgress.hpp:60-75, src/core/TChem_NetProductionRates.hpp:61-78), one
+ * mechanism per call, device arrays, stream-ordered. The rate constants follow the E3SM forms:
+ * ARRHENIUS and TROE without the ppm conversion factor, CMAQ_H2O2 with it
+ * (src/core/impl/TChem_Impl_KForward.hpp:44-147), JPL and R_JPL_ARRHENIUS with [M] = x(M)
+ * (src/core/impl/TChem_Impl_KForwardJPL.hpp:45-147), then the adjust_reaction factors in file
+ * order and the prod_O1D modifier (src/core/impl/TChem_Impl_AdjustReactions.hpp:45-100).
+ * Reactions 0 .. n_photo-1 without one of those rate types take photo_rates[s][r]
+ * (src/core/impl/TChem_Impl_RateofProgress.hpp:70-80); reactions with neither are 0. The net
+ * production rates of the active species start from external_sources[s][k]
+ * (src/core/impl/TChem_Impl_NetProductionRates.hpp:52-112). photo_rates (with n_photo = 0) and
+ * external_sources may be NULL (no photolysis input, zero sources).
+ *   kfor[nbatch][nReac], rop[nbatch][nReac], omega[nbatch][m] (active species). */
+int tchem_gb_e3sm_reaction_rates(const tchem_gb_mech* mech, int nbatch, const double* state,
+                                 const double* photo_rates, int n_photo, double* kfor, void* stream);
+int tchem_gb_e3sm_rate_of_progress(const tchem_gb_mech* mech, int nbatch, const double* state,
+                                   const double* photo_rates, int n_photo, double* rop, void* stream);
+int tchem_gb_e3sm_net_production_rates(const tchem_gb_mech* mech, int nbatch, const double* state,
+                                       const double* photo_rates, int n_photo, const double* external_sources,
+                                       double* omega, void* stream);
+/* E3SM time advance: tchem_gb_time_advance for one mechanism with the per-sample inputs
+ * photo_rates[nbatch][n_photo] and external_sources[nbatch][m], in any of the three forms. The
+ * rate constants are evaluated once per sample, so the species that scale them ([M] of the JPL
+ * forms, the adjust_reaction and prod_O1D species) must be constant species
+ * (TCHEM_GB_ERR_UNSUPPORTED otherwise; the E3SM mechanisms keep M, N2, O2 and H2O constant).
+ * The workspace also holds the per-sample rate constants: tchem_gb_e3sm_workspace_bytes. */
+size_t tchem_gb_e3sm_workspace_bytes(const tchem_gb_mech* mech, int nbatch, const tchem_gb_advance_opts* opts);
+int tchem_gb_e3sm_time_advance(const tchem_gb_mech* mech, int nbatch, const double* tol_newton,
+                               const double* tol_time, const double* fac, const tchem_gb_tadv* tadv,
+                               const double* state, const double* photo_rates, int n_photo,
+                               const double* external_sources, double* t_out, double* dt_out, double* state_out,
+                               int32_t* status, tchem_gb_sample_stats* stats, void* workspace,
+                               size_t workspace_bytes, const tchem_gb_advance_opts* opts, void* stream);
 
 /* Measurement helper (no counterpart in the reference): FMA throughput of the current device in
  * FLOP/s for FP64 (fp64 = 1) or FP32, from independent FMA chains on every SM. These are the

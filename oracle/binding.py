@@ -38,6 +38,14 @@ def load(native: bool = False) -> C.CDLL:
         L.oracle_adjoint.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, i]
         L.oracle_tangent.restype = i
         L.oracle_tangent.argtypes = [vp, i, vp, vp, vp, vp, vp, vp, i, vp, vp, vp, i]
+        d = C.c_double
+        for name in ("oracle_e3sm_kforward", "oracle_e3sm_rate_of_progress"):
+            getattr(L, name).restype = i
+            getattr(L, name).argtypes = [vp, vp, d, d, vp, vp, i, vp]
+        L.oracle_e3sm_net_production_rates.restype = i
+        L.oracle_e3sm_net_production_rates.argtypes = [vp, vp, d, d, vp, vp, i, vp, vp]
+        L.oracle_e3sm_time_advance.restype = i
+        L.oracle_e3sm_time_advance.argtypes = [vp, vp, i, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp, i, i, i]
         _libs[native] = L
     return _libs[native]
 
@@ -106,6 +114,64 @@ class Oracle:
                                           int(lu_fp32), int(bool(simplified)), int(nthreads))
         if rc != 0:
             raise RuntimeError(f"oracle_time_advance returned {rc}")
+        return state_out, t_out, dt_out, status, stats
+
+
+class E3smOracle:
+    """FP64 CPU restatement of the E3SM gas-chemistry rates and time advance for one kinetic model
+    (an object with ``view`` and ``e3sm_view`` attributes that outlives this one)."""
+
+    def __init__(self, model, native: bool = False):
+        self.model = model
+        self.lib = load(native)
+        self._km = C.cast(C.pointer(model.view), C.c_void_p)
+        self._e3 = C.cast(C.pointer(model.e3sm_view), C.c_void_p)
+        self.m = model.nSpec - model.nConstSpec
+
+    def _rates(self, fn, T, p, x, photo, n_out):
+        x = _a(x)
+        ph = None if photo is None or len(photo) == 0 else _a(photo)
+        out = np.zeros(n_out)
+        rc = fn(self._km, self._e3, float(T), float(p), _p(x), _p(ph), 0 if ph is None else ph.size, _p(out))
+        assert rc == 0, rc
+        return out
+
+    def kforward(self, T, p, x, photo=None) -> np.ndarray:
+        return self._rates(self.lib.oracle_e3sm_kforward, T, p, x, photo, self.model.nReac)
+
+    def rate_of_progress(self, T, p, x, photo=None) -> np.ndarray:
+        return self._rates(self.lib.oracle_e3sm_rate_of_progress, T, p, x, photo, self.model.nReac)
+
+    def net_production_rates(self, T, p, x, photo=None, ext=None) -> np.ndarray:
+        x = _a(x)
+        ph = None if photo is None or len(photo) == 0 else _a(photo)
+        out = np.zeros(self.m)
+        rc = self.lib.oracle_e3sm_net_production_rates(self._km, self._e3, float(T), float(p), _p(x), _p(ph),
+                                                       0 if ph is None else ph.size,
+                                                       _p(None if ext is None else _a(ext)), _p(out))
+        assert rc == 0, rc
+        return out
+
+    def time_advance(self, tadv, state, photo, ext, tol_newton, tol_time, t_out=None, lu_fp32: int = 0,
+                     simplified: bool = False, nthreads: int = 0):
+        """Returns (state_out, t_out, dt_out, status, stats); photo [B, n_photo] or None, ext [B, m] or None."""
+        B = state.shape[0]
+        state = _a(state)
+        state_out = state.copy()
+        t_out = np.array(tadv["tbeg"], dtype=np.float64) if t_out is None else np.array(t_out, dtype=np.float64)
+        dt_out = np.zeros(B)
+        status = np.zeros(B, dtype=np.int32)
+        from tchem_gb._capi import SAMPLE_STATS_DTYPE
+        stats = np.zeros(B, dtype=SAMPLE_STATS_DTYPE)
+        ph = None if photo is None or np.size(photo) == 0 else _a(photo)
+        n_photo = 0 if ph is None else ph.shape[1]
+        rc = self.lib.oracle_e3sm_time_advance(self._km, self._e3, B, _p(_a(tol_newton)), _p(_a(tol_time)),
+                                               _p(np.ascontiguousarray(tadv)), _p(state), _p(ph), n_photo,
+                                               _p(None if ext is None else _a(ext)), _p(t_out), _p(dt_out),
+                                               _p(state_out), _p(status), _p(stats), int(lu_fp32),
+                                               int(bool(simplified)), int(nthreads))
+        if rc != 0:
+            raise RuntimeError(f"oracle_e3sm_time_advance returned {rc}")
         return state_out, t_out, dt_out, status, stats
 
 

@@ -49,14 +49,93 @@ void kforward(const tchem_gb_kmcd_view& km, double t, double p, double* kfor) {
   }
 }
 
+// --- E3SM rate constants ---------------------------------------------------------------------
+// Order of src/core/impl/TChem_Impl_RateofProgress.hpp:70-80 and
+// src/core/impl/TChem_Impl_ReactionRates.hpp:54-79: photolysis rates into kfor[0, n_photo), then
+// KForward (src/core/impl/TChem_Impl_KForward.hpp:44-147: ARRHENIUS and TROE without the ppm
+// conversion, CMAQ_H2O2 with it), KForwardJPL (src/core/impl/TChem_Impl_KForwardJPL.hpp:45-147,
+// [M] = x(M_index)) and AdjustReactions (src/core/impl/TChem_Impl_AdjustReactions.hpp:45-100:
+// the adjust pairs serially in file order, then the prod_O1D modifier). x[nSpec]. Reactions
+// that neither list nor the photolysis input reaches stay 0.
+void e3sm_kforward(const tchem_gb_kmcd_view& km, const tchem_gb_e3sm_view& e3, double t, double p, const double* x,
+                   const double* photo, int n_photo, double* kfor) {
+  const double t_1 = 1.0 / t;
+  const double one = 1.0;
+  const double conv = km.CONV_PPM * p * t_1;
+  for (int r = 0; r < km.nReac; ++r) kfor[r] = (photo && r < n_photo) ? photo[r] : 0.0;
+  for (int i = 0; i < km.nArrhenius; ++i) {
+    const double* P = km.arrhenius_param + 5 * i;
+    const double E = P[0], A = P[1], B = P[2], C = P[3], D = P[4];
+    kfor[km.arrhenius_reaction[i]] =
+        A * std::exp(C * t_1) * (B == 0.0 ? one : std::pow(t / D, B)) * (E == 0.0 ? one : (one + E * p));
+  }
+  for (int i = 0; i < km.nTroe; ++i) {
+    const double* rp = km.reacPpar + 8 * i;
+    const double k0_A = rp[0], k0_B = rp[1], k0_C = rp[2];
+    const double kinf_A = rp[3], kinf_B = rp[4], kinf_C = rp[5], Fc = rp[6], N = rp[7];
+    const double k0 = k0_A * (k0_C == 0.0 ? one : std::exp(k0_C * t_1)) * (k0_B == 0.0 ? one : std::pow(t / 300.0, k0_B));
+    const double k0_kinf = k0 / (kinf_A * (kinf_C == 0.0 ? one : std::exp(kinf_C * t_1)) *
+                                 (kinf_B == 0.0 ? one : std::pow(t / 300.0, kinf_B)));
+    kfor[km.reacPfal[i]] = k0 / (1.0 + k0_kinf) * std::pow(Fc, 1.0 / (1.0 + std::pow(std::log10(k0_kinf) / N, 2.0)));
+  }
+  for (int i = 0; i < km.nCMAQ_H2O2; ++i) {
+    const double* P = km.cmaq_param + 6 * i;
+    const double A1 = P[0], B1 = P[1], C1 = P[2], A2 = P[3], B2 = P[4], C2 = P[5];
+    const int r = km.cmaq_reaction[i];
+    kfor[r] = (A1 * std::exp(C1 * t_1) * (B1 == 0.0 ? one : std::pow(t / 300.0, B1)) +
+               A2 * std::exp(C2 * t_1) * (B2 == 0.0 ? one : std::pow(t / 300.0, B2)) * conv) *
+              std::pow(conv, static_cast<double>(km.convExponent[r]));
+  }
+  const double mM = x[km.M_index];
+  // k0 and kinf of the JPL forms: A exp(C/T) (T/300)^B with the exp and pow skipped at C, B = 0
+  auto arr = [&](double A, double B, double C) {
+    return A * (C == 0.0 ? one : std::exp(C * t_1)) * (B == 0.0 ? one : std::pow(t / 300.0, B));
+  };
+  auto falloff = [&](const double* P) {  // k0_A, k0_B, k0_C, kinf_A, kinf_B, kinf_C, Fc
+    const double k0 = arr(P[0], P[1], P[2]);
+    const double kinf = arr(P[3], P[4], P[5]);
+    const double xpo = k0 * mM / kinf;
+    const double lg = std::log10(xpo);
+    const double factor = P[6] == one ? one : std::pow(P[6], one / (one + lg * lg));
+    return k0 / (one + xpo) * factor;
+  };
+  for (int i = 0; i < e3.nJPL; ++i) kfor[e3.jpl_reaction[i]] = falloff(e3.jpl_param + 7 * i);
+  for (int i = 0; i < e3.nRJPL; ++i) {
+    const double* P = e3.rjpl_param + 10 * i;
+    kfor[e3.rjpl_reaction[i]] = falloff(P) / arr(P[7], P[8], P[9]);
+  }
+  for (int i = 0; i < e3.nAdjust; ++i) kfor[e3.adjust_pair[2 * i]] *= x[e3.adjust_pair[2 * i + 1]];
+  for (int i = 0; i < e3.nProdO1D; ++i) {
+    const int32_t* I = e3.o1d_index + 7 * i;
+    const double* P = e3.o1d_param + 6 * i;
+    const double k1 = P[0] * std::exp(P[1] * t_1), k2 = P[2] * std::exp(P[3] * t_1), k3 = P[4] * std::exp(P[5] * t_1);
+    const double fc = k1 * x[I[4]] + k2 * x[I[5]] + k3 * x[I[6]];
+    for (int j = 0; j < 3; ++j) kfor[I[j]] *= kfor[I[3]] / fc;
+  }
+}
+
+// True when an active species scales a rate constant ([M] of the JPL forms, an adjust or a
+// prod_O1D species): the rate constants then change with the state.
+bool e3sm_kfor_depends_on_state(const tchem_gb_kmcd_view& km, const tchem_gb_e3sm_view& e3) {
+  const int m = km.nSpec - km.nConstSpec;
+  if ((e3.nJPL > 0 || e3.nRJPL > 0) && km.M_index < m) return true;
+  for (int i = 0; i < e3.nAdjust; ++i)
+    if (e3.adjust_pair[2 * i + 1] < m) return true;
+  for (int i = 0; i < e3.nProdO1D; ++i)
+    for (int j = 4; j < 7; ++j)
+      if (e3.o1d_index[7 * i + j] < m) return true;
+  return false;
+}
+
 // --- RHS: src/core/impl/TChem_Impl_ReactionRatesAerosol.hpp:57-143 --------------------------
-// concX[nSpec] (constant species last), kfor precomputed; omega[m].
+// concX[nSpec] (constant species last), kfor precomputed; omega[m]. src[m] (E3SM external
+// sources, src/core/impl/TChem_Impl_NetProductionRates.hpp:73-77) replaces the emissions.
 void reaction_rates(const tchem_gb_kmcd_view& km, const double* kfor, const double* concX, double* omega,
-                    double* rop) {
+                    double* rop, const double* src = nullptr) {
   const int m = km.nSpec - km.nConstSpec;
   const int S = km.maxSpecInReac;
-  for (int i = 0; i < m; ++i) omega[i] = 0.0;
-  for (int i = 0; i < km.nEmission; ++i) {
+  for (int i = 0; i < m; ++i) omega[i] = src ? src[i] : 0.0;
+  for (int i = 0; i < km.nEmission && !src; ++i) {
     const int k = km.emission_species[i];
     if (k < m) omega[k] = km.emission_rate[i];
   }
@@ -207,14 +286,22 @@ struct Sample {
   double* tape_dt = nullptr;
   int tape_cap = 0;
 
-  Sample(const tchem_gb_kmcd_view& km_, double T, double p, const double* xconst, const double* k_scale = nullptr)
-      : km(km_), m(km_.nSpec - km_.nConstSpec), n(km_.nSpec) {
+  // E3SM inputs: rate constants given per sample (kfor_in) and external sources (src) in place of
+  // the emissions.
+  const double* src = nullptr;
+
+  Sample(const tchem_gb_kmcd_view& km_, double T, double p, const double* xconst, const double* k_scale = nullptr,
+         const double* kfor_in = nullptr, const double* src_ = nullptr)
+      : km(km_), m(km_.nSpec - km_.nConstSpec), n(km_.nSpec), src(src_) {
     kfor.assign(km.nReac, 0.0);
     rop.assign(km.nReac, 0.0);
     concX.assign(n, 0.0);
     J.assign(static_cast<size_t>(m) * m, 0.0);
     for (int i = 0; i < n - m; ++i) concX[m + i] = xconst[i];
-    kforward(km, T, p, kfor.data());
+    if (kfor_in)
+      std::copy(kfor_in, kfor_in + km.nReac, kfor.begin());
+    else
+      kforward(km, T, p, kfor.data());
     if (k_scale)
       for (int r = 0; r < km.nReac; ++r) kfor[r] *= k_scale[r];
     lu.resize(m);
@@ -223,7 +310,7 @@ struct Sample {
   }
   void f(const double* y, double* out) {
     std::copy(y, y + m, concX.begin());
-    reaction_rates(km, kfor.data(), concX.data(), out, rop.data());
+    reaction_rates(km, kfor.data(), concX.data(), out, rop.data(), src);
     ++st.n_rhs;
   }
   void jac(const double* y) {
@@ -435,7 +522,8 @@ template <typename LU_T>
 void run_batch(const tchem_gb_kmcd_view* const* kms, const int32_t* mech_of_sample, int nbatch, const double* tol_newton,
                const double* tol_time, const tchem_gb_tadv* tadv, const double* state, double* t_out,
                double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats, int dim, int refine,
-               bool simplified) {
+               bool simplified, const tchem_gb_e3sm_view* e3 = nullptr, const double* photo = nullptr,
+               int n_photo = 0, const double* ext = nullptr) {
 #pragma omp parallel for schedule(dynamic, 1)
   for (int b = 0; b < nbatch; ++b) {
     const tchem_gb_kmcd_view& km = *kms[mech_of_sample ? mech_of_sample[b] : 0];
@@ -452,7 +540,17 @@ void run_batch(const tchem_gb_kmcd_view* const* kms, const int32_t* mech_of_samp
     const double rho = row[0], p = row[1], T = row[2];
     std::vector<double> y(row + 3, row + 3 + m);
     std::vector<double> xconst(row + 3 + m, row + 3 + n);
-    Sample<LU_T> smp(km, T, p, xconst.data());
+    // E3SM: rate constants once per sample at the initial state (they depend on constant
+    // species only), external sources (zero when none are given) in place of the emissions.
+    std::vector<double> kfor_e3, src_e3;
+    if (e3) {
+      kfor_e3.assign(km.nReac, 0.0);
+      e3sm_kforward(km, *e3, T, p, row + 3, photo ? photo + static_cast<size_t>(b) * n_photo : nullptr, n_photo,
+                    kfor_e3.data());
+      src_e3.assign(m, 0.0);
+      if (ext) std::copy(ext + static_cast<size_t>(b) * m, ext + static_cast<size_t>(b + 1) * m, src_e3.begin());
+    }
+    Sample<LU_T> smp(km, T, p, xconst.data(), nullptr, e3 ? kfor_e3.data() : nullptr, e3 ? src_e3.data() : nullptr);
     Settings s{ta.max_num_newton_iterations, std::max(1, ta.jacobian_interval), ta.num_time_iterations_per_interval,
                refine, simplified, tol_newton[0], tol_newton[1], tol_time};
     double to = 0.0, dto = 0.0;
@@ -669,6 +767,59 @@ int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const
   else
     run_batch<double>(kms, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status,
                       stats, dim, 0, simplified != 0);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(prev);
+#endif
+  return TCHEM_GB_OK;
+}
+
+int oracle_e3sm_kforward(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_view* e3, double T, double p,
+                         const double* x, const double* photo, int n_photo, double* kfor) {
+  if (!km || !e3 || !x || !kfor || n_photo < 0) return TCHEM_GB_ERR_ARG;
+  e3sm_kforward(*km, *e3, T, p, x, photo, photo ? n_photo : 0, kfor);
+  return TCHEM_GB_OK;
+}
+
+int oracle_e3sm_rate_of_progress(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_view* e3, double T, double p,
+                                 const double* x, const double* photo, int n_photo, double* rop) {
+  if (!km || !e3 || !x || !rop || n_photo < 0) return TCHEM_GB_ERR_ARG;
+  std::vector<double> kfor(km->nReac), omega(km->nSpec - km->nConstSpec), zero(km->nSpec - km->nConstSpec, 0.0);
+  e3sm_kforward(*km, *e3, T, p, x, photo, photo ? n_photo : 0, kfor.data());
+  reaction_rates(*km, kfor.data(), x, omega.data(), rop, zero.data());
+  return TCHEM_GB_OK;
+}
+
+int oracle_e3sm_net_production_rates(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_view* e3, double T, double p,
+                                     const double* x, const double* photo, int n_photo, const double* ext,
+                                     double* omega) {
+  if (!km || !e3 || !x || !omega || n_photo < 0) return TCHEM_GB_ERR_ARG;
+  const int m = km->nSpec - km->nConstSpec;
+  std::vector<double> kfor(km->nReac), rop(km->nReac), zero(m, 0.0);
+  e3sm_kforward(*km, *e3, T, p, x, photo, photo ? n_photo : 0, kfor.data());
+  reaction_rates(*km, kfor.data(), x, omega, rop.data(), ext ? ext : zero.data());
+  return TCHEM_GB_OK;
+}
+
+int oracle_e3sm_time_advance(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_view* e3, int nbatch,
+                             const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
+                             const double* state, const double* photo, int n_photo, const double* ext, double* t_out,
+                             double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats,
+                             int lu_fp32, int simplified, int nthreads) {
+  if (!km || !e3 || nbatch < 0 || n_photo < 0 || !tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out ||
+      !state_out)
+    return TCHEM_GB_ERR_ARG;
+  if (e3sm_kfor_depends_on_state(*km, *e3)) return TCHEM_GB_ERR_UNSUPPORTED;
+  const tchem_gb_kmcd_view* kms[1] = {km};
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+  if (lu_fp32)
+    run_batch<float>(kms, nullptr, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status, stats,
+                     km->nSpec + 3, lu_fp32 - 1, simplified != 0, e3, photo, photo ? n_photo : 0, ext);
+  else
+    run_batch<double>(kms, nullptr, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status, stats,
+                      km->nSpec + 3, 0, simplified != 0, e3, photo, photo ? n_photo : 0, ext);
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(prev);
 #endif

@@ -56,6 +56,35 @@ int oracle_time_advance(const tchem_gb_kmcd_view* const* kms, int n_mechs, const
                         const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
                         tchem_gb_sample_stats* stats, int lu_fp32, int simplified, int nthreads);
 
+/* E3SM gas chemistry (the engine's tchem_gb_e3sm_* entry points), one sample per call for the
+ * rates, x[nSpec] (constant species last), photo[n_photo] (NULL: none):
+ *   oracle_e3sm_kforward          rate constants: photolysis rates into kfor[0, n_photo), then
+ *                                 src/core/impl/TChem_Impl_KForward.hpp:44-147 (ARRHENIUS and TROE
+ *                                 without the ppm conversion), TChem_Impl_KForwardJPL.hpp:45-147 and
+ *                                 TChem_Impl_AdjustReactions.hpp:45-100, in the order of
+ *                                 src/core/impl/TChem_Impl_RateofProgress.hpp:70-80 and
+ *                                 TChem_Impl_ReactionRates.hpp:54-79
+ *   oracle_e3sm_rate_of_progress  rop[nReac], src/core/impl/TChem_Impl_RateofProgress.hpp:84-98
+ *   oracle_e3sm_net_production_rates
+ *                                 omega[m] from ext[m] (NULL: zero) plus the stoichiometric sums,
+ *                                 src/core/impl/TChem_Impl_NetProductionRates.hpp:52-112
+ *   oracle_e3sm_time_advance      oracle_time_advance (one mechanism) with these rates, per-sample
+ *                                 photo[nbatch][n_photo] and ext[nbatch][m]; rate constants once per
+ *                                 sample (TCHEM_GB_ERR_UNSUPPORTED when an active species scales
+ *                                 one, as the engine). */
+int oracle_e3sm_kforward(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_view* e3, double T, double p,
+                         const double* x, const double* photo, int n_photo, double* kfor);
+int oracle_e3sm_rate_of_progress(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_view* e3, double T, double p,
+                                 const double* x, const double* photo, int n_photo, double* rop);
+int oracle_e3sm_net_production_rates(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_view* e3, double T, double p,
+                                     const double* x, const double* photo, int n_photo, const double* ext,
+                                     double* omega);
+int oracle_e3sm_time_advance(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_view* e3, int nbatch,
+                             const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
+                             const double* state, const double* photo, int n_photo, const double* ext, double* t_out,
+                             double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats,
+                             int lu_fp32, int simplified, int nthreads);
+
 /* Discrete adjoint of the plain form on a recorded step sequence (the engine's
  * tchem_gb_time_advance_record / tchem_gb_adjoint), restated densely on the CPU, one mechanism:
  *   oracle_time_advance_record: oracle_time_advance (FP64) recording the accepted step sizes

@@ -17,6 +17,7 @@ constexpr int kTapeSegment = 32;    // steps between trajectory checkpoints (adj
 struct MixedLayout {
   uint32_t warp_bytes;
   uint32_t x, keff, q, x32, keff32, d32, ustage, lrow, pinv, piv, ybuf, vec, stats, red, item;
+  uint32_t src;  // [m] the sample's E3SM source term (E3SM instantiations only; else 0)
   int32_t LDU, LDL;
   int32_t simplified;  // 1: simplified-Newton form; 2: full Newton on the Gauss-Jordan inverse; 0: LU
 };
@@ -54,6 +55,11 @@ struct AdvanceParams {
   int32_t* tape_nsteps;                         // [B]
   int32_t tape_cap;
   const double* k_scale;                        // [R] rate-constant multipliers (null: none)
+  // E3SM inputs (null: the mechanism's rate constants and emissions): per-sample effective rate
+  // constants (constant-species factors included) and source terms, row s at src_in + s * src_stride.
+  const double* keff_in;                        // [B][R]
+  const double* src_in;                         // [B][m] (src_stride m) or one zero row (src_stride 0)
+  int64_t src_stride;
 };
 
 }  // namespace tchem_gb

@@ -75,8 +75,10 @@ struct Plan {
 };
 
 // Groups structurally identical mechanisms and sizes each group's launch.
+// e3sm: the E3SM time advance (per-sample rate constants and source terms): every rate form of
+// the E3SM tables is allowed, and each warp group gets a source-term section.
 Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool have_mos, const tchem_gb_advance_opts& o,
-               int dev) {
+               int dev, bool e3sm = false) {
   if (n_mechs <= 0 || n_mechs > kMaxMechs) throw std::invalid_argument("n_mechs must be in [1, 64]");
   Plan plan;
   std::vector<const HostTables*> hts(n_mechs);
@@ -85,7 +87,12 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
     if (!mechs[i]) throw std::invalid_argument("null mechanism handle");
     dts[i] = tables_for(mechs[i], dev);
     hts[i] = mechs[i]->host_tables.get();
-    if (!hts[i]->supported) throw std::domain_error(hts[i]->unsupported_reason);
+    if (e3sm) {
+      if (!hts[i]->e3sm_valid) throw std::domain_error(hts[i]->e3sm_invalid_reason);
+      if (!hts[i]->e3sm_state_free) throw std::domain_error(hts[i]->e3sm_reason);
+    } else if (!hts[i]->supported) {
+      throw std::domain_error(hts[i]->unsupported_reason);
+    }
   }
   for (int i = 0; i < n_mechs; ++i) {
     bool placed = false;
@@ -121,7 +128,7 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
       int tps = o.threads_per_sample;
       if (tps == 0 && o.form >= 0 && o.form < 3) tps = mechs[g.mechs[0]]->tps_pref[o.form];
       MixedConfig mc = mixed_config(L, tps, info.sm_count, info.max_smem_optin, nbatch,
-                                    o.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED);
+                                    o.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED, e3sm);
       g.kernel = mc.kernel;
       g.warps_per_block = mc.warps_per_block;
       g.grid = mc.grid;
@@ -133,12 +140,12 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
       continue;
     }
     g.lda = L.m | 1;
-    size_t ws = fp64_warp_smem_bytes(L, g.lda, true);
+    size_t ws = fp64_warp_smem_bytes(L, g.lda, true, e3sm);
     const size_t avail = static_cast<size_t>(info.max_smem_optin) - 16 - L.blob_bytes;
     int W = static_cast<int>(std::min<size_t>(kMaxWarpsPerBlock, avail / ws));
     if (W < 1) {
       g.matrix_in_smem = false;
-      ws = fp64_warp_smem_bytes(L, g.lda, false);
+      ws = fp64_warp_smem_bytes(L, g.lda, false, e3sm);
       W = static_cast<int>(std::min<size_t>(kMaxWarpsPerBlock, avail / ws));
       if (W < 1) throw std::invalid_argument("mechanism too large for the shared-memory working set");
     }
@@ -256,11 +263,19 @@ struct TapeArgs {
   const double* k_scale = nullptr;
 };
 
+// E3SM inputs of the time-advance kernels (all null: the mechanism's rates and emissions).
+struct RateArgs {
+  const double* keff = nullptr;  // [B][R]
+  const double* src = nullptr;   // source rows, row s at src + s * src_stride
+  int64_t src_stride = 0;
+};
+
 int time_advance_impl(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
                       const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
                       const double* state, double* t_out, double* dt_out, double* state_out, int32_t* status,
                       tchem_gb_sample_stats* stats, void* workspace, size_t workspace_bytes,
-                      const tchem_gb_advance_opts* opts, void* stream_v, const TapeArgs& tape) {
+                      const tchem_gb_advance_opts* opts, void* stream_v, const TapeArgs& tape,
+                      const RateArgs& rates = RateArgs{}) {
   if (!mechs || nbatch < 0) return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance: bad mechanisms or batch size");
   if (nbatch == 0) return TCHEM_GB_OK;  // empty arrays may come with null pointers
   if (!tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out || !state_out || !status)
@@ -273,7 +288,7 @@ int time_advance_impl(const tchem_gb_mech* const* mechs, int n_mechs, const int3
   cudaGetDevice(&dev);
   Plan plan;
   try {
-    plan = make_plan(mechs, n_mechs, nbatch, mech_of_sample != nullptr, o, dev);
+    plan = make_plan(mechs, n_mechs, nbatch, mech_of_sample != nullptr, o, dev, rates.keff != nullptr);
     const int n0 = mechs[0]->km.nSpec;
     for (int i = 1; i < n_mechs; ++i)
       if (mechs[i]->km.nSpec + 3 > n0 + 3 && mech_of_sample == nullptr)
@@ -349,6 +364,9 @@ int time_advance_impl(const tchem_gb_mech* const* mechs, int n_mechs, const int3
     P.tape_nsteps = tape.nsteps;
     P.tape_cap = tape.cap;
     P.k_scale = tape.k_scale;
+    P.keff_in = rates.keff;
+    P.src_in = rates.src;
+    P.src_stride = rates.src_stride;
     if (gp.form == TCHEM_GB_FORM_MIXED || gp.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED)
       e = launch_trbdf2_mixed(P, gp.dev.L, gp.grid, gp.warps_per_block, gp.smem, gp.threads_per_sample, stream);
     else
@@ -755,6 +773,166 @@ int tchem_gb_time_advance_hostbuf(const tchem_gb_mech* const* mechs, int n_mechs
   if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
   if (e != cudaSuccess) return cuda_fail(e, "tchem_gb_time_advance_hostbuf: device-to-host copy");
   return TCHEM_GB_OK;
+}
+
+}  // extern "C"
+
+// ---- E3SM gas chemistry -----------------------------------------------------------------------
+
+namespace tchem_gb {
+namespace {
+
+// Tables of one mechanism for the E3SM kernels (throws domain_error when they cannot drive them).
+const DeviceTables* e3sm_tables(const tchem_gb_mech* mech, int dev) {
+  if (!mech) throw std::invalid_argument("null mechanism");
+  const DeviceTables* t = tables_for(mech, dev);
+  if (!mech->host_tables->e3sm_valid) throw std::domain_error(mech->host_tables->e3sm_invalid_reason);
+  return t;
+}
+
+int run_e3sm_rates(const tchem_gb_mech* mech, int nbatch, const double* state, const double* photo_rates, int n_photo,
+                   const double* external_sources, double* out, void* stream_v, E3smOut kind, const char* who) {
+  if (!mech || nbatch < 0 || n_photo < 0 || (n_photo > 0 && !photo_rates))
+    return fail(TCHEM_GB_ERR_ARG, std::string(who) + ": bad argument");
+  if (nbatch == 0) return TCHEM_GB_OK;
+  if (!state || !out) return fail(TCHEM_GB_ERR_ARG, std::string(who) + ": null array");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  E3smParams P{};
+  try {
+    P.mech = e3sm_tables(mech, dev)->dev;
+  } catch (const std::domain_error& e) {
+    return fail(TCHEM_GB_ERR_UNSUPPORTED, e.what());
+  } catch (const std::exception& e) {
+    return fail(TCHEM_GB_ERR_ARG, e.what());
+  }
+  P.B = nbatch;
+  P.state = state;
+  P.state_dim = mech->km.nSpec + 3;
+  P.photo = n_photo > 0 ? photo_rates : nullptr;
+  P.n_photo = n_photo;
+  P.ext = external_sources;
+  P.out = out;
+  const cudaError_t e = launch_e3sm(P, kind, device_info(dev).sm_count, static_cast<cudaStream_t>(stream_v));
+  if (e != cudaSuccess) return cuda_fail(e, who);
+  return TCHEM_GB_OK;
+}
+
+// Workspace of the E3SM time advance: the time-advance plan, then keff[B][R], then one zero row of
+// m source terms (used when the caller passes no external sources).
+struct E3smLayout {
+  size_t plan_bytes = 0, keff_offset = 0, zero_offset = 0, bytes = 0;
+};
+
+E3smLayout e3sm_layout(const tchem_gb_mech* mech, int nbatch, const tchem_gb_advance_opts& o, int dev) {
+  e3sm_tables(mech, dev);
+  const tchem_gb_mech* mechs[1] = {mech};
+  E3smLayout l;
+  l.plan_bytes = make_plan(mechs, 1, nbatch, false, o, dev, true).bytes;
+  l.keff_offset = up256(l.plan_bytes);
+  l.zero_offset = l.keff_offset + up256(sizeof(double) * static_cast<size_t>(std::max(nbatch, 1)) * mech->km.nReac);
+  l.bytes = l.zero_offset + up256(sizeof(double) * mech->km.nActive());
+  return l;
+}
+
+}  // namespace
+}  // namespace tchem_gb
+
+extern "C" {
+
+int tchem_gb_e3sm_reaction_rates(const tchem_gb_mech* mech, int nbatch, const double* state,
+                                 const double* photo_rates, int n_photo, double* kfor, void* stream) {
+  return run_e3sm_rates(mech, nbatch, state, photo_rates, n_photo, nullptr, kfor, stream, E3SM_KFOR,
+                        "tchem_gb_e3sm_reaction_rates");
+}
+
+int tchem_gb_e3sm_rate_of_progress(const tchem_gb_mech* mech, int nbatch, const double* state,
+                                   const double* photo_rates, int n_photo, double* rop, void* stream) {
+  return run_e3sm_rates(mech, nbatch, state, photo_rates, n_photo, nullptr, rop, stream, E3SM_ROP,
+                        "tchem_gb_e3sm_rate_of_progress");
+}
+
+int tchem_gb_e3sm_net_production_rates(const tchem_gb_mech* mech, int nbatch, const double* state,
+                                       const double* photo_rates, int n_photo, const double* external_sources,
+                                       double* omega, void* stream) {
+  return run_e3sm_rates(mech, nbatch, state, photo_rates, n_photo, external_sources, omega, stream, E3SM_OMEGA,
+                        "tchem_gb_e3sm_net_production_rates");
+}
+
+size_t tchem_gb_e3sm_workspace_bytes(const tchem_gb_mech* mech, int nbatch, const tchem_gb_advance_opts* opts) {
+  try {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return e3sm_layout(mech, nbatch, opts_or_default(opts), dev).bytes;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return 0;
+  }
+}
+
+int tchem_gb_e3sm_time_advance(const tchem_gb_mech* mech, int nbatch, const double* tol_newton,
+                               const double* tol_time, const double* /*fac*/, const tchem_gb_tadv* tadv,
+                               const double* state, const double* photo_rates, int n_photo,
+                               const double* external_sources, double* t_out, double* dt_out, double* state_out,
+                               int32_t* status, tchem_gb_sample_stats* stats, void* workspace,
+                               size_t workspace_bytes, const tchem_gb_advance_opts* opts, void* stream_v) {
+  if (!mech || nbatch < 0 || n_photo < 0 || (n_photo > 0 && !photo_rates))
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_e3sm_time_advance: bad argument");
+  if (nbatch == 0) return TCHEM_GB_OK;
+  if (!tol_newton || !tol_time || !tadv || !state || !t_out || !dt_out || !state_out || !status)
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_e3sm_time_advance: null argument");
+  const tchem_gb_advance_opts o = opts_or_default(opts);
+  if (o.form != TCHEM_GB_FORM_PLAIN_FP64 && o.form != TCHEM_GB_FORM_MIXED && o.form != TCHEM_GB_FORM_MIXED_SIMPLIFIED)
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_e3sm_time_advance: unknown form");
+  int dev = 0;
+  cudaGetDevice(&dev);
+  E3smLayout l;
+  try {
+    l = e3sm_layout(mech, nbatch, o, dev);
+  } catch (const std::domain_error& e) {
+    return fail(TCHEM_GB_ERR_UNSUPPORTED, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(TCHEM_GB_ERR_NOMEM, "tchem_gb_e3sm_time_advance: allocation failed");
+  } catch (const std::exception& e) {
+    return fail(TCHEM_GB_ERR_ARG, e.what());
+  }
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  if (!ws) {
+    try {
+      ws = static_cast<unsigned char*>(owned_workspace(dev, l.bytes));
+    } catch (...) {
+      return fail(TCHEM_GB_ERR_NOMEM, "tchem_gb_e3sm_time_advance: workspace allocation failed");
+    }
+    workspace_bytes = l.bytes;
+  } else if (workspace_bytes < l.bytes) {
+    return fail(TCHEM_GB_ERR_ARG, "tchem_gb_e3sm_time_advance: workspace smaller than tchem_gb_e3sm_workspace_bytes()");
+  }
+  cudaStream_t stream = static_cast<cudaStream_t>(stream_v);
+  double* keff = reinterpret_cast<double*>(ws + l.keff_offset);
+  E3smParams E{};
+  E.mech = mech->device_tables[dev]->dev;
+  E.B = nbatch;
+  E.state = state;
+  E.state_dim = mech->km.nSpec + 3;
+  E.photo = n_photo > 0 ? photo_rates : nullptr;
+  E.n_photo = n_photo;
+  E.out = keff;
+  cudaError_t e = launch_e3sm(E, E3SM_KEFF, device_info(dev).sm_count, stream);
+  if (e != cudaSuccess) return cuda_fail(e, "E3SM rate-constant kernel launch");
+  RateArgs ra;
+  ra.keff = keff;
+  if (external_sources) {
+    ra.src = external_sources;
+    ra.src_stride = mech->km.nActive();
+  } else {
+    ra.src = reinterpret_cast<const double*>(ws + l.zero_offset);
+    ra.src_stride = 0;
+    e = cudaMemsetAsync(ws + l.zero_offset, 0, sizeof(double) * mech->km.nActive(), stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(workspace)");
+  }
+  const tchem_gb_mech* mechs[1] = {mech};
+  return time_advance_impl(mechs, 1, nullptr, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out,
+                           status, stats, ws, workspace_bytes, &o, stream_v, TapeArgs{}, ra);
 }
 
 }  // extern "C"

@@ -70,6 +70,46 @@ void tchem_gb_mech::build_view() {
   view.nEmission = static_cast<int32_t>(emission_species.size());
   view.emission_species = emission_species.data();
   view.emission_rate = emission_rate.data();
+
+  jpl_reaction.clear();
+  jpl_param.clear();
+  for (const auto& j : k.jpl) {
+    jpl_reaction.push_back(j.reaction_index);
+    const double p[7] = {j.k0_A, j.k0_B, j.k0_C, j.kinf_A, j.kinf_B, j.kinf_C, j.Fc};
+    jpl_param.insert(jpl_param.end(), p, p + 7);
+  }
+  rjpl_reaction.clear();
+  rjpl_param.clear();
+  for (const auto& j : k.r_jpl_arrhenius) {
+    rjpl_reaction.push_back(j.reaction_index);
+    const double p[10] = {j.k0_A, j.k0_B, j.k0_C, j.kinf_A, j.kinf_B, j.kinf_C, j.Fc, j.A, j.B, j.C};
+    rjpl_param.insert(rjpl_param.end(), p, p + 10);
+  }
+  adjust_pair.clear();
+  for (const auto& a : k.adjust_reaction) {
+    adjust_pair.push_back(a.reaction_index);
+    adjust_pair.push_back(a.species_index);
+  }
+  o1d_index.clear();
+  o1d_param.clear();
+  for (const auto& o : k.prod_O1D) {
+    const int32_t idx[7] = {o.reaction_indices[0], o.reaction_indices[1], o.reaction_indices[2],
+                            o.photolysis_reaction_index, o.species_index_1, o.species_index_2, o.species_index_3};
+    o1d_index.insert(o1d_index.end(), idx, idx + 7);
+    const double p[6] = {o.A1, o.C1, o.A2, o.C2, o.A3, o.C3};
+    o1d_param.insert(o1d_param.end(), p, p + 6);
+  }
+  e3sm_view.nJPL = static_cast<int32_t>(jpl_reaction.size());
+  e3sm_view.jpl_reaction = jpl_reaction.data();
+  e3sm_view.jpl_param = jpl_param.data();
+  e3sm_view.nRJPL = static_cast<int32_t>(rjpl_reaction.size());
+  e3sm_view.rjpl_reaction = rjpl_reaction.data();
+  e3sm_view.rjpl_param = rjpl_param.data();
+  e3sm_view.nAdjust = static_cast<int32_t>(k.adjust_reaction.size());
+  e3sm_view.adjust_pair = adjust_pair.data();
+  e3sm_view.nProdO1D = static_cast<int32_t>(k.prod_O1D.size());
+  e3sm_view.o1d_index = o1d_index.data();
+  e3sm_view.o1d_param = o1d_param.data();
 }
 
 tchem_gb_mech::~tchem_gb_mech() {
@@ -136,6 +176,15 @@ int tchem_gb_mech_host_view(const tchem_gb_mech* mech, tchem_gb_kmcd_view* view)
   return TCHEM_GB_OK;
 }
 
+int tchem_gb_mech_e3sm_view(const tchem_gb_mech* mech, tchem_gb_e3sm_view* view) {
+  if (!mech || !view) {
+    set_last_error("tchem_gb_mech_e3sm_view: null argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  *view = mech->e3sm_view;
+  return TCHEM_GB_OK;
+}
+
 int tchem_gb_mech_species_name(const tchem_gb_mech* mech, int i, char* buf, int buflen) {
   if (!mech || !buf || buflen <= 0 || i < 0 || i >= mech->km.nSpec) {
     set_last_error("tchem_gb_mech_species_name: bad argument");
@@ -179,6 +228,41 @@ int tchem_gb_scenario_read(const char* yaml_path, const tchem_gb_mech* mech, dou
       return TCHEM_GB_ERR_ARG;
     }
     std::memcpy(state_host, state.data(), state.size() * sizeof(double));
+    return TCHEM_GB_OK;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return TCHEM_GB_ERR_PARSE;
+  }
+}
+
+int tchem_gb_scenario_photolysis_rates(const char* yaml_path, int nbatch, double* photo_host, int* n_photo) {
+  if (!yaml_path || !n_photo || nbatch < 0) {
+    set_last_error("tchem_gb_scenario_photolysis_rates: bad argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  try {
+    std::vector<double> photo;
+    tchem_gb::setScenarioPhotolysisRates(yaml_path, nbatch, photo, *n_photo);
+    if (photo_host && !photo.empty()) std::memcpy(photo_host, photo.data(), photo.size() * sizeof(double));
+    return TCHEM_GB_OK;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return TCHEM_GB_ERR_PARSE;
+  }
+}
+
+int tchem_gb_scenario_external_forcing(const char* yaml_path, const tchem_gb_mech* mech, int nbatch,
+                                       double* ext_host, int* count) {
+  if (!yaml_path || !mech || !ext_host || nbatch < 0) {
+    set_last_error("tchem_gb_scenario_external_forcing: bad argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  try {
+    std::vector<double> ext;
+    int c = 0;
+    tchem_gb::setScenarioExternalForcing(yaml_path, mech->km, nbatch, ext, c);
+    if (!ext.empty()) std::memcpy(ext_host, ext.data(), ext.size() * sizeof(double));
+    if (count) *count = c;
     return TCHEM_GB_OK;
   } catch (const std::exception& e) {
     set_last_error(e.what());

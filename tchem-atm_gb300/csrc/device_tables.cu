@@ -113,6 +113,72 @@ HostTables build_host_tables(const KineticModel& km) {
     }
   }
 
+  // E3SM rate tables.
+  ht.e3_type.assign(R, E3_NONE);
+  ht.e3_param.assign(static_cast<size_t>(R) * kE3smParams, 0.0);
+  auto e3p = [&](int r) { return &ht.e3_param[static_cast<size_t>(r) * kE3smParams]; };
+  for (const auto& a : km.arrhenius) {
+    ht.e3_type[a.reaction_index] = E3_ARRHENIUS;
+    double* p = e3p(a.reaction_index);
+    p[0] = a.A; p[1] = a.B; p[2] = a.C; p[3] = a.D; p[4] = a.E;
+  }
+  for (size_t i = 0; i < km.reacPfal.size(); ++i) {
+    ht.e3_type[km.reacPfal[i]] = E3_TROE;
+    for (int k = 0; k < 8; ++k) e3p(km.reacPfal[i])[k] = km.reacPpar[i * 8 + k];
+  }
+  for (const auto& c : km.cmaq_h2o2) {
+    ht.e3_type[c.reaction_index] = E3_CMAQ_H2O2;
+    double* p = e3p(c.reaction_index);
+    p[0] = c.A1; p[1] = c.B1; p[2] = c.C1; p[3] = c.A2; p[4] = c.B2; p[5] = c.C2;
+  }
+  for (const auto& j : km.jpl) {
+    ht.e3_type[j.reaction_index] = E3_JPL;
+    double* p = e3p(j.reaction_index);
+    p[0] = j.k0_A; p[1] = j.k0_B; p[2] = j.k0_C; p[3] = j.kinf_A; p[4] = j.kinf_B; p[5] = j.kinf_C; p[6] = j.Fc;
+  }
+  for (const auto& j : km.r_jpl_arrhenius) {
+    ht.e3_type[j.reaction_index] = E3_RJPL;
+    double* p = e3p(j.reaction_index);
+    p[0] = j.k0_A; p[1] = j.k0_B; p[2] = j.k0_C; p[3] = j.kinf_A; p[4] = j.kinf_B; p[5] = j.kinf_C; p[6] = j.Fc;
+    p[7] = j.A; p[8] = j.B; p[9] = j.C;
+  }
+  for (const auto& a : km.adjust_reaction) {
+    ht.e3_adj.push_back(a.reaction_index);
+    ht.e3_adj.push_back(a.species_index);
+    if (a.species_index < m) {
+      ht.e3sm_state_free = false;
+      ht.e3sm_reason = "adjust_reaction of reaction " + std::to_string(a.reaction_index) + " names the active species " +
+                       km.speciesNames[a.species_index];
+    }
+  }
+  for (const auto& o : km.prod_O1D) {
+    const int32_t idx[7] = {o.reaction_indices[0], o.reaction_indices[1], o.reaction_indices[2],
+                            o.photolysis_reaction_index, o.species_index_1, o.species_index_2, o.species_index_3};
+    bool in_range = true;
+    for (int k = 0; k < 7; ++k) in_range = in_range && idx[k] >= 0 && idx[k] < (k < 4 ? R : n);
+    if (!in_range) {
+      ht.e3sm_valid = false;
+      ht.e3sm_invalid_reason = "modifier_prod_O1D: a reaction or species index is out of range";
+      continue;
+    }
+    ht.e3_o1d.insert(ht.e3_o1d.end(), idx, idx + 7);
+    const double par[6] = {o.A1, o.C1, o.A2, o.C2, o.A3, o.C3};
+    ht.e3_o1d_par.insert(ht.e3_o1d_par.end(), par, par + 6);
+    for (int k = 4; k < 7; ++k)
+      if (idx[k] < m) {
+        ht.e3sm_state_free = false;
+        ht.e3sm_reason = "modifier_prod_O1D names the active species " + km.speciesNames[idx[k]];
+      }
+  }
+  ht.M_index = km.M_index;
+  if ((!km.jpl.empty() || !km.r_jpl_arrhenius.empty()) && km.M_index < m) {
+    ht.e3sm_state_free = false;
+    ht.e3sm_reason = "the JPL rate forms read [M] and M is an active species";
+  }
+  if (!ht.e3sm_state_free)
+    ht.e3sm_reason += ": the E3SM time advance evaluates rate constants once per sample and needs them to depend "
+                      "on constant species only";
+
   // Factor slots (rate of progress) and constant-species factors.
   std::vector<int32_t> rf_ptr(R + 1, 0);
   std::vector<int16_t> rf_sp;
@@ -303,6 +369,11 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   const size_t o_rxs = sec(sizeof(int32_t) * ht.rx_sidx.size());
   const size_t o_rxnu = sec(sizeof(double) * ht.rx_nu.size());
   const size_t o_rxn = sec(sizeof(int32_t) * ht.rx_n.size());
+  const size_t o_e3t = sec(sizeof(int32_t) * R);
+  const size_t o_e3p = sec(sizeof(double) * R * kE3smParams);
+  const size_t o_e3a = sec(sizeof(int32_t) * std::max<size_t>(1, ht.e3_adj.size()));
+  const size_t o_e3o = sec(sizeof(int32_t) * std::max<size_t>(1, ht.e3_o1d.size()));
+  const size_t o_e3op = sec(sizeof(double) * std::max<size_t>(1, ht.e3_o1d_par.size()));
   std::vector<unsigned char> host(off, 0);
   std::memcpy(host.data() + o_blob, ht.blob.data(), ht.blob.size());
   std::memcpy(host.data() + o_blob_x, ht.blob_x.data(), ht.blob_x.size());
@@ -314,6 +385,12 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   std::memcpy(host.data() + o_rxs, ht.rx_sidx.data(), sizeof(int32_t) * ht.rx_sidx.size());
   std::memcpy(host.data() + o_rxnu, ht.rx_nu.data(), sizeof(double) * ht.rx_nu.size());
   std::memcpy(host.data() + o_rxn, ht.rx_n.data(), sizeof(int32_t) * ht.rx_n.size());
+  std::memcpy(host.data() + o_e3t, ht.e3_type.data(), sizeof(int32_t) * R);
+  std::memcpy(host.data() + o_e3p, ht.e3_param.data(), sizeof(double) * R * kE3smParams);
+  if (!ht.e3_adj.empty()) std::memcpy(host.data() + o_e3a, ht.e3_adj.data(), sizeof(int32_t) * ht.e3_adj.size());
+  if (!ht.e3_o1d.empty()) std::memcpy(host.data() + o_e3o, ht.e3_o1d.data(), sizeof(int32_t) * ht.e3_o1d.size());
+  if (!ht.e3_o1d_par.empty())
+    std::memcpy(host.data() + o_e3op, ht.e3_o1d_par.data(), sizeof(double) * ht.e3_o1d_par.size());
 
   int prev = 0;
   cudaGetDevice(&prev);
@@ -346,6 +423,14 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   t->dev.rx_nu = reinterpret_cast<const double*>(b + o_rxnu);
   t->dev.rx_n = reinterpret_cast<const int32_t*>(b + o_rxn);
   t->dev.rx_S = ht.rx_S;
+  t->dev.e3_type = reinterpret_cast<const int32_t*>(b + o_e3t);
+  t->dev.e3_param = reinterpret_cast<const double*>(b + o_e3p);
+  t->dev.e3_adj = reinterpret_cast<const int32_t*>(b + o_e3a);
+  t->dev.e3_o1d = reinterpret_cast<const int32_t*>(b + o_e3o);
+  t->dev.e3_o1d_par = reinterpret_cast<const double*>(b + o_e3op);
+  t->dev.e3_nadj = static_cast<int32_t>(ht.e3_adj.size() / 2);
+  t->dev.e3_no1d = static_cast<int32_t>(ht.e3_o1d.size() / 7);
+  t->dev.M_index = ht.M_index;
   t->dev_x = t->dev;
   t->dev_x.L = ht.Lx;
   t->dev_x.blob = b + o_blob_x;

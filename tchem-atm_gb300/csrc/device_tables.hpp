@@ -26,6 +26,11 @@ namespace tchem_gb {
 
 enum DevRateType : int32_t { RATE_ARRHENIUS = 0, RATE_TROE = 1, RATE_CMAQ_H2O2 = 2, RATE_ZERO = 3 };
 
+// Rate forms of the E3SM gas chemistry (kernels_e3sm.cu); E3_NONE reactions take the photolysis
+// input or 0.
+enum E3smRateType : int32_t { E3_NONE = 0, E3_ARRHENIUS = 1, E3_TROE = 2, E3_CMAQ_H2O2 = 3, E3_JPL = 4, E3_RJPL = 5 };
+constexpr int kE3smParams = 10;  // parameters per reaction in MechDev::e3_param
+
 // Byte offsets of each section inside the staged blob (16-byte aligned sections).
 struct MechLayout {
   int32_t m, n, nconst, R, NF, NP, NZ, NC;
@@ -61,6 +66,15 @@ struct MechDev {
   const double* rx_nu;     // [R][rx_S], reactants signed negative, products from rx_S / 2
   const int32_t* rx_n;     // [R][2]: number of reactants, products
   int32_t rx_S;
+  // E3SM rate tables. e3_param per form: ARRHENIUS A, B, C, D, E; TROE the 8 reacPpar values;
+  // CMAQ_H2O2 A1, B1, C1, A2, B2, C2; JPL k0_A, k0_B, k0_C, kinf_A, kinf_B, kinf_C, Fc; R_JPL the
+  // JPL values then A, B, C.
+  const int32_t* e3_type;     // [R] E3smRateType
+  const double* e3_param;     // [R][kE3smParams]
+  const int32_t* e3_adj;      // [e3_nadj][2]: reaction, species (applied in this order)
+  const int32_t* e3_o1d;      // [e3_no1d][7]: reactions 1..3, photolysis reaction, species 1..3
+  const double* e3_o1d_par;   // [e3_no1d][6]: A1, C1, A2, C2, A3, C3
+  int32_t e3_nadj, e3_no1d, M_index;
 };
 
 // Host-side packed tables, built from a parsed kinetic model.
@@ -78,6 +92,15 @@ struct HostTables {
   std::vector<int64_t> signature;
   bool supported = true;     // false when the mechanism has rate types outside the box path
   std::string unsupported_reason;
+  // E3SM tables (MechDev::e3_*); e3sm_state_free: no active species scales a rate constant, so
+  // the E3SM time advance may evaluate them once per sample.
+  std::vector<int32_t> e3_type, e3_adj, e3_o1d;
+  std::vector<double> e3_param, e3_o1d_par;
+  int32_t M_index = -1;
+  bool e3sm_valid = true;  // false: the tables cannot drive the E3SM kernels (reason below)
+  std::string e3sm_invalid_reason;
+  bool e3sm_state_free = true;
+  std::string e3sm_reason;
 };
 
 HostTables build_host_tables(const KineticModel& km);

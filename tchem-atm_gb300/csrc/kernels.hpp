@@ -8,7 +8,7 @@
 namespace tchem_gb {
 
 // Plain FP64 form (kernels_fp64.cu).
-size_t fp64_warp_smem_bytes(const MechLayout& L, int lda, bool matrix_in_smem);
+size_t fp64_warp_smem_bytes(const MechLayout& L, int lda, bool matrix_in_smem, bool src_section = false);
 cudaError_t launch_trbdf2_fp64(const AdvanceParams& P, int grid, int warps_per_block, size_t smem,
                                cudaStream_t stream);
 const void* trbdf2_fp64_kernel_ptr(int m);
@@ -60,6 +60,20 @@ struct UnitParams {
 };
 enum UnitKind { UNIT_KFORWARD = 0, UNIT_RHS = 1, UNIT_JACOBIAN = 2 };
 cudaError_t launch_unit(const UnitParams& P, UnitKind kind, cudaStream_t stream);
+
+// E3SM gas-chemistry rates (kernels_e3sm.cu): one warp per sample, grid-stride over samples.
+enum E3smOut { E3SM_KFOR = 0, E3SM_ROP = 1, E3SM_OMEGA = 2, E3SM_KEFF = 3 };
+struct E3smParams {
+  MechDev mech;            // plain-form tables (CSR net-production program) and e3_* tables
+  int32_t B;
+  const double* state;     // [B][state_dim]
+  int32_t state_dim;
+  const double* photo;     // [B][n_photo] or null
+  int32_t n_photo;
+  const double* ext;       // [B][m] or null (E3SM_OMEGA)
+  double* out;             // kfor, rop, keff [B][R]; omega [B][m]
+};
+cudaError_t launch_e3sm(const E3smParams& P, E3smOut kind, int sm_count, cudaStream_t stream);
 
 // Groups samples by mechanism group: items[g * B + k], counts[g] (kernels_fp64.cu).
 struct GroupMap {

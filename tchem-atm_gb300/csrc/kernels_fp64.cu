@@ -16,9 +16,10 @@ namespace tchem_gb {
 
 using namespace fp64;
 
-size_t fp64_warp_smem_bytes(const MechLayout& L, int lda, bool matrix_in_smem) {
+size_t fp64_warp_smem_bytes(const MechLayout& L, int lda, bool matrix_in_smem, bool src_section) {
   auto up16 = [](size_t b) { return (b + 15) & ~size_t(15); };
   size_t b = 0;
+  if (src_section) b += up16(sizeof(double) * L.m);  // per-sample source term
   b += up16(sizeof(double) * L.m);   // x
   b += up16(sizeof(double) * L.R);   // keff
   b += up16(sizeof(double) * L.R);   // q
@@ -39,10 +40,16 @@ __global__ void __launch_bounds__(256, 1) trbdf2_fp64_kernel(const __grid_consta
     if (threadIdx.x == 0) atomicOr(P.error_word, kErrBarrierTimeout);
     return;
   }
-  const SmemTables T = tables_at(tables, L);
+  SmemTables T = tables_at(tables, L);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   unsigned char* mine = tables + L.blob_bytes + static_cast<size_t>(warp) * P.warp_smem_bytes;
   auto up16 = [](size_t b) { return (b + 15) & ~size_t(15); };
+  double* src = nullptr;  // per-sample source term (E3SM external sources) in place of the emissions
+  if (P.src_in) {
+    src = reinterpret_cast<double*>(mine);
+    mine += up16(sizeof(double) * L.m);
+    T.emis = src;
+  }
   WarpMem W;
   W.x = reinterpret_cast<double*>(mine);
   mine += up16(sizeof(double) * L.m);
@@ -88,7 +95,13 @@ __global__ void __launch_bounds__(256, 1) trbdf2_fp64_kernel(const __grid_consta
     }
     const double* row = P.state + static_cast<size_t>(s) * P.state_dim;
     const double p = row[1], Tk = row[2];
-    compute_keff(P.mech, P.rate_param[slot], Tk, p, row + 3 + m, W.keff, lane);
+    if (P.keff_in) {
+      for (int r = lane; r < L.R; r += 32) W.keff[r] = P.keff_in[static_cast<size_t>(s) * L.R + r];
+    } else {
+      compute_keff(P.mech, P.rate_param[slot], Tk, p, row + 3 + m, W.keff, lane);
+    }
+    if (P.src_in)
+      for (int i = lane; i < m; i += 32) src[i] = P.src_in[s * P.src_stride + i];
     __syncwarp();
     if (P.k_scale) {
       for (int r = lane; r < L.R; r += 32) W.keff[r] *= P.k_scale[r];

@@ -17,8 +17,9 @@ struct MixedConfig {
   MixedLayout ml{};
 };
 
+// e3: the E3SM instantiations (per-sample rate constants and source terms).
 MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch,
-                         bool simplified);
+                         bool simplified, bool e3 = false);
 cudaError_t launch_trbdf2_mixed(const AdvanceParams& P, const MechLayout& L, int grid, int warps_per_block,
                                 size_t smem, int threads_per_sample, cudaStream_t stream);
 

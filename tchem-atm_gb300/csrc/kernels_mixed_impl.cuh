@@ -46,7 +46,8 @@ enum Vec { V_FN = 0, V_FG = 1, V_YP = 2, V_ATOL = 3, V_RTOL = 4, V_YGP = 5, kVec
 // Work counters kept in shared memory, in tchem_gb_sample_stats order.
 enum Stat { S_STEPS = 0, S_REJ = 1, S_NFAIL = 2, S_NEWTON = 3, S_LU = 4, S_SOLVE = 5, S_RHS = 6, S_JAC = 7 };
 
-inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified) {
+// src_section: a per-group source-term section (the E3SM kernels' per-sample external sources).
+inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified, bool src_section = false) {
   auto up16 = [](size_t b) { return static_cast<uint32_t>((b + 15) & ~size_t(15)); };
   MixedLayout ml{};
   ml.LDU = ldu_for(MC);
@@ -69,6 +70,8 @@ inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified) {
   ml.stats = o; o += up16(sizeof(int) * 8);
   ml.red = o; o += 256;  // cross-warp reductions of multi-warp samples (2 x 8 u32, 2 x 8 f64, 2 f32)
   ml.item = o; o += up16(sizeof(int) * 4);
+  ml.src = 0;
+  if (src_section) { ml.src = o; o += up16(sizeof(double) * L.m); }
   ml.warp_bytes = o;
   return ml;
 }
@@ -81,11 +84,15 @@ inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified) {
 // group's warps, and reductions and the pivot broadcast go through shared memory with a named
 // barrier per group.
 //
+// E3 selects the E3SM inputs: per-sample rate constants (P.keff_in) and source terms (P.src_in,
+// staged into the group's shared memory) instead of the mechanism's rate parameters and emissions.
+// A separate instantiation, so the other kernels compile exactly as without it.
+//
 // FULLGJ (with SIMP) keeps the Gauss-Jordan linear algebra but runs the reference's full Newton
 // (a new matrix every jacobian_interval iterations, the reference's stage guesses and 2-norm
 // test) with one FP64-residual refinement sweep per solve, like the FP32-LU form: it follows the
 // FP64 Newton iterates with matrix-vector solves instead of triangular ones.
-template <int MC, int RPT, bool SIMP, int G = 1, bool FULLGJ = false>
+template <int MC, int RPT, bool SIMP, int G = 1, bool FULLGJ = false, bool E3 = false>
 struct Solver {
   static_assert(!FULLGJ || SIMP, "the full-Newton Gauss-Jordan variant uses the inverse");
   static constexpr bool kSimplifiedNewton = SIMP && !FULLGJ;
@@ -246,7 +253,11 @@ struct Solver {
     const int32_t* ws_off = t<int32_t>(L.off_ws_off);
     const int16_t* wse_r = t<int16_t>(L.off_wse_r);
     const double* wse_nu = t<double>(L.off_wse_nu);
-    const double* emis = t<double>(L.off_emis);
+    const double* emis;
+    if constexpr (E3)
+      emis = w<double>(P.ml.src);  // the sample's E3SM source term
+    else
+      emis = t<double>(L.off_emis);
 #pragma unroll 2
     for (int sl = wslice(); sl < L.NWS; sl += G) {
       const int sp = ws_sp[sl * 32 + lane];
@@ -1106,13 +1117,13 @@ struct Solver {
 // Shapes with one row per thread hold half the matrix registers of the two-rows-per-lane shapes,
 // so they fit 168 registers and run 12 warps per SM (the 52-column two-warp shape 128 registers
 // and 16 warps); the others run 8.
-template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false>
+template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false, bool E3 = false>
 constexpr int max_threads() {
   return (RPT == 1 && MC <= 52 && G == 2) ? 512 : ((RPT == 1 && MC <= 64) ? 384 : 256);
 }
 
-template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false>
-__global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G, FULLGJ>(), 1)
+template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false, bool E3 = false>
+__global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G, FULLGJ, E3>(), 1)
     trbdf2_mixed_kernel(const __grid_constant__ AdvanceParams P) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
@@ -1124,7 +1135,7 @@ __global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G, FULLGJ>(), 1)
   }
   constexpr int NT = 32 * G;
   const int group = threadIdx.x / NT, tid = threadIdx.x % NT, lane = threadIdx.x & 31;
-  Solver<MC, RPT, SIMP, G, FULLGJ> S{P, tables, tables + L.blob_bytes + group * P.ml.warp_bytes, lane, tid, tid >> 5,
+  Solver<MC, RPT, SIMP, G, FULLGJ, E3> S{P, tables, tables + L.blob_bytes + group * P.ml.warp_bytes, lane, tid, tid >> 5,
                              1 + group};
   const int m = L.m;
   const int n_items = P.n_items_dev ? *P.n_items_dev : P.n_items;
@@ -1156,7 +1167,15 @@ __global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G, FULLGJ>(), 1)
     }
     const double* row = P.state + static_cast<size_t>(smp) * P.state_dim;
     const double p = row[1], Tk = row[2];
-    {
+    if constexpr (E3) {
+      for (int r = tid; r < L.R; r += NT) {
+        const double k = P.keff_in[static_cast<size_t>(smp) * L.R + r];
+        keff[r] = k;
+        keff32[r] = static_cast<float>(k);
+      }
+      double* src = S.template w<double>(P.ml.src);
+      for (int i = tid; i < m; i += NT) src[i] = P.src_in[smp * P.src_stride + i];
+    } else {
       const double t_1 = 1.0 / Tk;
       const double conv = P.mech.conv_ppm * p * t_1;
       const double* rp = P.rate_param[slot];

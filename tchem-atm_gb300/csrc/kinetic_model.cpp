@@ -387,4 +387,49 @@ void setScenarioConditions(const std::string& path, const KineticModel& km, std:
   }
 }
 
+void setScenarioPhotolysisRates(const std::string& path, int nBatch, std::vector<double>& photo, int& nPhoto) {
+  yaml::NodePtr root = yaml::parse_file(path);
+  nPhoto = 0;
+  photo.clear();
+  const Node* rates = root->get("photolysis_rates");
+  if (!rates) return;
+  nPhoto = static_cast<int>(rates->size());
+  photo.assign(static_cast<size_t>(nBatch) * nPhoto, 0.0);
+  for (int r = 0; r < nPhoto; ++r) {
+    const std::string key = "r_" + std::to_string(r);
+    const Node* entry = rates->get(key);
+    const Node* vals = entry ? entry->get("value") : nullptr;
+    if (!vals || static_cast<int>(vals->size()) != nBatch)
+      throw std::runtime_error("Error number of values in photo reaction is different than number of conditions (" +
+                               key + ")");
+    for (int b = 0; b < nBatch; ++b) photo[static_cast<size_t>(b) * nPhoto + r] = vals->seq[b]->as_double();
+  }
+}
+
+void setScenarioExternalForcing(const std::string& path, const KineticModel& km, int nBatch, std::vector<double>& ext,
+                                int& count) {
+  yaml::NodePtr root = yaml::parse_file(path);
+  const int m = km.nActive();
+  ext.assign(static_cast<size_t>(nBatch) * m, 0.0);
+  count = 0;
+  const Node* forcing = root->get("external_forcing");
+  if (!forcing) return;
+  if (m == 0 || nBatch == 0) throw std::runtime_error("Number of active species and bacthes is zero.");
+  for (const auto& kv : forcing->map) {
+    const std::string name = req(kv.second.get(), "species_name", "external_forcing")->as_string();
+    int idx = -1;  // active species only, first match on the stored (truncated) names
+    for (int i = 0; i < m; ++i)
+      if (std::strncmp(km.speciesNames[i].c_str(), name.c_str(), LENGTHOFSPECNAME) == 0) {
+        idx = i;
+        break;
+      }
+    if (idx < 0) throw std::runtime_error("species " + name + " does not exits in tchem species lists.");
+    const Node* vals = kv.second->get("value");
+    if (!vals || static_cast<int>(vals->size()) != nBatch)
+      throw std::runtime_error("Error number of values in external forcing is different than number of conditions");
+    for (int b = 0; b < nBatch; ++b) ext[static_cast<size_t>(b) * m + idx] = vals->seq[b]->as_double();
+    ++count;
+  }
+}
+
 }  // namespace tchem_gb

@@ -112,4 +112,15 @@ struct KineticModel {
 // where conv = CONV_PPM * p / T.
 void setScenarioConditions(const std::string& path, const KineticModel& km, std::vector<double>& state, int& nBatch);
 
+// Photolysis-rate reader (src/core/TChem_AtmosphericChemistry.cpp:512-559): photo[nBatch][nPhoto]
+// from photolysis_rates.r_0 .. r_{nPhoto-1}.value, nPhoto = the number of entries of that
+// section (0 without it). Every list must hold nBatch values.
+void setScenarioPhotolysisRates(const std::string& path, int nBatch, std::vector<double>& photo, int& nPhoto);
+
+// External-forcing reader (src/core/TChem_AtmosphericChemistry.cpp:562-631): ext[nBatch][m],
+// zero except the active species named by external_forcing entries (species_name, value list of
+// nBatch values; a later entry for the same species overwrites). count = number of entries.
+void setScenarioExternalForcing(const std::string& path, const KineticModel& km, int nBatch, std::vector<double>& ext,
+                                int& count);
+
 }  // namespace tchem_gb

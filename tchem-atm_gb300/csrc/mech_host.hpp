@@ -24,6 +24,10 @@ struct tchem_gb_mech {
   std::vector<int32_t> arrhenius_reaction, cmaq_reaction, emission_species, reacPfal;
   std::vector<double> arrhenius_param, cmaq_param, emission_rate;
   tchem_gb_kmcd_view view{};
+  // Flattened copies backing tchem_gb_e3sm_view.
+  std::vector<int32_t> jpl_reaction, rjpl_reaction, adjust_pair, o1d_index;
+  std::vector<double> jpl_param, rjpl_param, o1d_param;
+  tchem_gb_e3sm_view e3sm_view{};
   // Packed tables (built on first device use) and their device copies per CUDA device ordinal.
   std::unique_ptr<tchem_gb::HostTables> host_tables;
   std::vector<tchem_gb::DeviceTables*> device_tables;

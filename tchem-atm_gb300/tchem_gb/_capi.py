@@ -42,6 +42,15 @@ class KmcdView(C.Structure):
     ]
 
 
+class E3smView(C.Structure):
+    _fields_ = [
+        ("nJPL", C.c_int32), ("jpl_reaction", C.POINTER(C.c_int32)), ("jpl_param", C.POINTER(C.c_double)),
+        ("nRJPL", C.c_int32), ("rjpl_reaction", C.POINTER(C.c_int32)), ("rjpl_param", C.POINTER(C.c_double)),
+        ("nAdjust", C.c_int32), ("adjust_pair", C.POINTER(C.c_int32)),
+        ("nProdO1D", C.c_int32), ("o1d_index", C.POINTER(C.c_int32)), ("o1d_param", C.POINTER(C.c_double)),
+    ]
+
+
 class AdvanceOpts(C.Structure):
     _fields_ = [("form", C.c_int32), ("threads_per_sample", C.c_int32), ("reserved", C.c_int32 * 6)]
 
@@ -77,6 +86,9 @@ def lib() -> C.CDLL:
         "tchem_gb_mech_species_name": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int]),
         "tchem_gb_scenario_batch_size": (C.c_int, [C.c_char_p, C.POINTER(C.c_int)]),
         "tchem_gb_scenario_read": (C.c_int, [C.c_char_p, vp, vp, C.c_int]),
+        "tchem_gb_mech_e3sm_view": (C.c_int, [vp, C.POINTER(E3smView)]),
+        "tchem_gb_scenario_photolysis_rates": (C.c_int, [C.c_char_p, C.c_int, vp, C.POINTER(C.c_int)]),
+        "tchem_gb_scenario_external_forcing": (C.c_int, [C.c_char_p, vp, C.c_int, vp, C.POINTER(C.c_int)]),
     }
     popts = C.POINTER(AdvanceOpts)
     optional = {
@@ -98,6 +110,12 @@ def lib() -> C.CDLL:
         "tchem_gb_mech_set_threads_per_sample": (C.c_int, [vp, C.c_int, C.c_int]),
         "tchem_gb_adjoint": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp,
                                        C.c_size_t, vp]),
+        "tchem_gb_e3sm_reaction_rates": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, vp, vp]),
+        "tchem_gb_e3sm_rate_of_progress": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, vp, vp]),
+        "tchem_gb_e3sm_net_production_rates": (C.c_int, [vp, C.c_int, vp, vp, C.c_int, vp, vp, vp]),
+        "tchem_gb_e3sm_workspace_bytes": (C.c_size_t, [vp, C.c_int, popts]),
+        "tchem_gb_e3sm_time_advance": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp,
+                                                 vp, vp, C.c_size_t, popts, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

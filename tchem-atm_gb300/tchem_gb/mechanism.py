@@ -22,6 +22,9 @@ class KineticModel:
         v = _capi.KmcdView()
         _capi.check(_capi.lib().tchem_gb_mech_host_view(self._h, C.byref(v)), "tchem_gb_mech_host_view")
         self._view = v
+        e = _capi.E3smView()
+        _capi.check(_capi.lib().tchem_gb_mech_e3sm_view(self._h, C.byref(e)), "tchem_gb_mech_e3sm_view")
+        self._e3sm_view = e
         self.nSpec = v.nSpec
         self.nConstSpec = v.nConstSpec
         self.nReac = v.nReac
@@ -57,6 +60,11 @@ class KineticModel:
     def view(self) -> _capi.KmcdView:
         """Reference-layout host tables (valid while this object lives)."""
         return self._view
+
+    @property
+    def e3sm_view(self) -> _capi.E3smView:
+        """The E3SM rate tables (JPL, R_JPL_ARRHENIUS, adjust_reaction, prod_O1D), same lifetime."""
+        return self._e3sm_view
 
     @property
     def n_active(self) -> int:
@@ -99,3 +107,27 @@ def set_scenario_conditions(yaml_path: str | Path, km: KineticModel) -> np.ndarr
                                                    state.ctypes.data_as(C.c_void_p), nb),
                 "tchem_gb_scenario_read")
     return state
+
+
+def set_scenario_photolysis_rates(yaml_path: str | Path, nbatch: int) -> np.ndarray:
+    """photo_rates[nBatch, nPhoto] from a scenario file's photolysis_rates section
+    (AtmChemistry::setScenarioConditionsPhotolysisReactions); nPhoto = 0 without one."""
+    n = C.c_int()
+    _capi.check(_capi.lib().tchem_gb_scenario_photolysis_rates(str(yaml_path).encode(), nbatch, None, C.byref(n)),
+                "tchem_gb_scenario_photolysis_rates")
+    photo = np.zeros((nbatch, n.value), dtype=np.float64)
+    _capi.check(_capi.lib().tchem_gb_scenario_photolysis_rates(str(yaml_path).encode(), nbatch,
+                                                               photo.ctypes.data_as(C.c_void_p), C.byref(n)),
+                "tchem_gb_scenario_photolysis_rates")
+    return photo
+
+
+def set_scenario_external_forcing(yaml_path: str | Path, km: KineticModel, nbatch: int) -> np.ndarray:
+    """external_sources[nBatch, m] from a scenario file's external_forcing section
+    (AtmChemistry::setScenarioConditionsExternalForcing); zero where none is given."""
+    ext = np.zeros((nbatch, km.n_active), dtype=np.float64)
+    count = C.c_int()
+    _capi.check(_capi.lib().tchem_gb_scenario_external_forcing(str(yaml_path).encode(), km.handle, nbatch,
+                                                               ext.ctypes.data_as(C.c_void_p), C.byref(count)),
+                "tchem_gb_scenario_external_forcing")
+    return ext

@@ -9,7 +9,12 @@ Everything copied is data the reference's own tests and examples use:
   * the CB05CL_AE5 TR-BDF2 golden (src/unit-tests/CB05CL_AE5/references/full_gas.hdf5), read
     without h5py at its raw data offset (3 x 87 little-endian doubles at byte 2048),
   * the reference's TR-BDF2 trajectory of the Emission case (Emissions.dat) and the CAMP
-    analytic/solver result tables of the small test mechanisms (*_results.txt).
+    analytic/solver result tables of the small test mechanisms (*_results.txt),
+  * the E3SM goldens of the reference's gtests: the rate constant, rate-of-progress and
+    net-production-rate files (src/unit-tests/references/{reaction_rates,rate_of_progress,
+    net_production_rates}/*.dat, compared as text), the 80-column uci scenario they and the E3SM
+    time advance read (photolysis rates and external forcing included), and that time advance's
+    end states (src/unit-tests/references/atmospheric_chemistry_e3sm/uci_col/full_gas.dat).
 Run settings of each case come from the reference's scripts and are recorded in manifest.json.
 """
 from __future__ import annotations
@@ -70,6 +75,22 @@ def main(ref: Path) -> None:
     for name, (src, _) in camp.items():
         np.save(HERE / f"camp_{name}.npy", np.loadtxt(ref / RUNS / src))
 
+    e3sm_dir = HERE / "e3sm"
+    e3sm_dir.mkdir(exist_ok=True)
+    e3sm_copies = {
+        "uci_col_input_conditions.yaml": f"{RUNS}/uci_col/input_conditions_col.yaml",
+        "reaction-rates.dat": "src/unit-tests/references/reaction_rates/reaction-rates.dat",
+        "rate-of-progress.dat": "src/unit-tests/references/rate_of_progress/rate-of-progress.dat",
+        "net-production-rates.dat": "src/unit-tests/references/net_production_rates/net-production-rates.dat",
+        "uci_col_net_production_rates.dat":
+            "src/unit-tests/references/net_production_rates/uci_col/net_production_rates.dat",
+    }
+    for dst, src in e3sm_copies.items():
+        shutil.copyfile(ref / src, e3sm_dir / dst)
+    full_gas = np.genfromtxt(ref / "src/unit-tests/references/atmospheric_chemistry_e3sm/uci_col/full_gas.dat",
+                             skip_header=1)
+    np.save(e3sm_dir / "uci_col_full_gas.npy", full_gas)
+
     manifest = {
         "cb05cl_ae5_full_gas": {
             "source": "src/unit-tests/CB05CL_AE5/references/full_gas.hdf5",
@@ -91,6 +112,32 @@ def main(ref: Path) -> None:
                         "settings": {"tend": 100, "dtmin": 1e-20, "dtmax": 0.1, "output_every": 1.0}}
                  for name, (src, rt) in camp.items()},
         "echo": {dst: src for dst, src in echoes.items()},
+        "e3sm": {
+            "files": {f"e3sm/{dst}": src for dst, src in e3sm_copies.items()},
+            "reaction-rates.dat": {"run": "src/unit-tests/TChem_Test_ReactionRates.hpp:28-50",
+                                   "mechanism": "mechanisms/uci.yaml", "sample": 0,
+                                   "criterion": "byte-identical text (TChem::Test::compareFiles)"},
+            "rate-of-progress.dat": {"run": "src/unit-tests/TChem_Test_RateofProgress.hpp:28-50",
+                                     "mechanism": "mechanisms/uci_v2.yaml", "sample": 0,
+                                     "criterion": "byte-identical text (TChem::Test::compareFiles)"},
+            "net-production-rates.dat": {"run": "src/unit-tests/TChem_Test_NetProductionRates.hpp:28-51",
+                                         "mechanism": "mechanisms/uci_v2.yaml", "sample": 0,
+                                         "criterion": "byte-identical text (TChem::Test::compareFiles)"},
+            "uci_col_net_production_rates.dat": {
+                "run": "src/unit-tests/TChem_Test_NetProductionRates.hpp:54-79",
+                "mechanism": "mechanisms/uci_v2_test3.yaml", "scenario": "e3sm/uci_col_input_conditions.yaml",
+                "criterion": "byte-identical text (TChem::Test::compareFiles)"},
+            "uci_col_full_gas.npy": {
+                "source": "src/unit-tests/references/atmospheric_chemistry_e3sm/uci_col/full_gas.dat",
+                "run": "src/unit-tests/TChem_Test_AtmosphericChemistryE3SM.hpp:56-93",
+                "mechanism": "mechanisms/uci_v2_test3.yaml", "scenario": "e3sm/uci_col_input_conditions.yaml",
+                "rows": "80 initial rows (iter -1) then 80 rows after one runDeviceBatch call (iter 0)",
+                "settings": {"tbeg": 0, "tend": 1800, "dt_in": 1e-20, "dtmin": 1e-20, "dtmax": 3600,
+                             "iters_per_interval": 100, "atol_newton": 1e-18, "rtol_newton": 1e-8,
+                             "max_newton": 20, "atol_time": 1e-12, "rtol_time": 1e-6, "jacobian_interval": 1},
+                "criterion": "TChem::Test::compareFilesValues: relative error at the largest absolute "
+                             "difference <= 1e-8 (src/core/TChem_Util.hpp:1130-1180)"},
+        },
     }
     (HERE / "manifest.json").write_text(json.dumps(manifest, indent=1) + "\n")
     print(f"fixtures written to {HERE}")

@@ -54,3 +54,30 @@ def host_time_loop(advance, state: np.ndarray, tadv: np.ndarray, tend: float, ma
         tsum = float(np.mean(t))
         it += 1
     return np.array(rows), state
+
+
+def compare_files_values(test: np.ndarray, ref: np.ndarray) -> float:
+    """The criterion of TChem::Test::compareFilesValues (src/core/TChem_Util.hpp:1130-1180): the
+    relative error |test - ref| / ref at the element with the largest absolute difference."""
+    d = np.abs(np.asarray(test, dtype=np.float64) - np.asarray(ref, dtype=np.float64))
+    i = np.unravel_index(int(d.argmax()), d.shape)
+    return float(d[i] / abs(ref[i])) if d[i] > 0 else 0.0
+
+
+def format_reaction_rates(values, n: int) -> str:
+    """Text of TChem::Test::writeReactionRates (src/core/TChem_Util.hpp:1036-1049): a header
+    naming n and the vector length, then 'index   value' lines in std::scientific (6 digits)."""
+    return f"## nSpec({n})    Omega({len(values)})\n" + "".join(f"{i}   {v:e}\n" for i, v in enumerate(values))
+
+
+def format_2d_matrix(mat: np.ndarray) -> str:
+    """Text of TChem::Test::write2DMatrix (src/core/TChem_Util.hpp:1098-1118): two header lines, then
+    each row's values in std::scientific, each followed by one space."""
+    r, c = mat.shape
+    return (f"## nRows({r})    ({r})\n## nCols({c})    ({c})\n" +
+            "".join("".join(f"{v:e} " for v in row) + "\n" for row in mat))
+
+
+def tolerance_units(test: np.ndarray, ref: np.ndarray, atol: float, rtol: float) -> np.ndarray:
+    """|test - ref| in units of the time-step tolerance atol + rtol |ref|."""
+    return np.abs(test - ref) / (atol + rtol * np.abs(ref))
