@@ -17,6 +17,10 @@ Metric: box-samples/s = samples advanced to the horizon per second (whole job, a
 end-to-end pass through the host-buffer C ABI with host<->device copies inside the timed region
 (e2e), the plain FP64 form on a subsample, the CPU oracle on a bounded subsample (cpu_baseline)
 and the end-state error of the chosen form against the FP64 results.
+The E3SM leg ("e3sm") times AtmosphericChemistryE3SM::runDeviceBatch on the reference's
+80-column uci scenario (photolysis rates and external forcing as per-sample inputs) in the three
+forms, the NetProductionRates kernel, the CPU restatement on the host cores, and checks the end
+states against the reference's golden.
 --impl reference times the reference algorithm's CPU restatement (the oracle, FP64, OpenMP on all
 host threads) on a bounded subsample per step; the reference's own Kokkos build cannot be built
 here (Kokkos, Tines, Sacado and yaml-cpp are absent).
@@ -80,6 +84,8 @@ def parse() -> argparse.Namespace:
                          "autotuned shapes, one CUDA-graph launch; 0 skips it")
     ap.add_argument("--adjoint-samples", type=int, default=8192,
                     help="samples of the discrete-adjoint leg (1800 s horizon, FP64); 0 skips it")
+    ap.add_argument("--e3sm-samples", type=int, default=65536,
+                    help="samples of the E3SM leg (the reference's 80-column uci scenario tiled); 0 skips it")
     return ap.parse_args()
 
 
@@ -333,6 +339,103 @@ def uneven_leg(B: int, dev, stream) -> dict:
             "autotuned": tuned}
 
 
+# ---- E3SM gas chemistry -----------------------------------------------------------------------
+
+E3SM_MECH = ROOT / "tests" / "golden" / "mechanisms" / "uci_v2_test3.yaml"
+E3SM_SCENARIO = ROOT / "tests" / "golden" / "e3sm" / "uci_col_input_conditions.yaml"
+E3SM_GOLDEN = ROOT / "tests" / "golden" / "e3sm" / "uci_col_full_gas.npy"
+
+
+def e3sm_leg(B: int, cpu_seconds: float, dev, stream) -> dict:
+    """The E3SM TR-BDF2 advance (AtmosphericChemistryE3SM::runDeviceBatch) of the reference's
+    80-column uci scenario (53 active species, 106 reactions, 22 photolysis rates, external
+    forcing) tiled to B samples, with the settings of the reference's E3SM gtest (1800 s, dt_in =
+    dt_min = 1e-20, dt_max = 3600, rtol 1e-6, at most 100 steps per call); the NetProductionRates
+    kernel on the same rows; the CPU restatement on the host cores; the first 80 end states against
+    the reference's golden."""
+    import torch
+    from oracle import E3smOracle
+    from tchem_gb import (set_scenario_conditions, set_scenario_external_forcing, set_scenario_photolysis_rates,
+                          tadv_to_device)
+    from tchem_gb.e3sm import AtmosphericChemistryE3SM, NetProductionRates
+    km = KineticModel.from_file(E3SM_MECH)
+    base = set_scenario_conditions(E3SM_SCENARIO, km)
+    nc, m = base.shape[0], km.n_active
+    rep = -(-B // nc)
+    state = np.tile(base, (rep, 1))[:B]
+    photo = np.tile(set_scenario_photolysis_rates(E3SM_SCENARIO, nc), (rep, 1))[:B]
+    ext = np.tile(set_scenario_external_forcing(E3SM_SCENARIO, km, nc), (rep, 1))[:B]
+    tadv = np.zeros(B, dtype=_capi.TIME_ADVANCE_DTYPE)
+    tadv["tbeg"], tadv["tend"], tadv["dt"], tadv["dtmin"], tadv["dtmax"] = 0.0, 1800.0, 1e-20, 1e-20, 3600.0
+    tadv["max_num_newton_iterations"] = 20
+    tadv["num_time_iterations_per_interval"] = 100
+    tadv["jacobian_interval"] = 1
+    tol_time = np.tile([ATOL, RTOL], (m, 1))
+    d = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    d_state, d_photo, d_ext, d_tadv = d(state), d(photo), d(ext), tadv_to_device(tadv, dev)
+    d_tn, d_tt = torch.tensor(TOL_NEWTON, dtype=torch.float64, device=dev), d(tol_time)
+    out = torch.empty_like(d_state)
+    t = torch.zeros(B, dtype=torch.float64, device=dev)
+    dt = torch.zeros_like(t)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def timed(fn, reps: int = 3) -> float:
+        fn()  # warm-up: tables on the device, kernel attributes, workspace
+        best = float("inf")
+        for _ in range(reps):
+            ev[0].record(stream)
+            fn()
+            ev[1].record(stream)
+            torch.cuda.synchronize(dev)
+            best = min(best, ev[0].elapsed_time(ev[1]))
+        return best
+
+    forms, results = {}, {}
+    for form, tps in (("simplified", 32), ("simplified", 64), ("mixed", 32), ("plain", 0)):
+        def run(form=form, tps=tps):
+            t.zero_()
+            AtmosphericChemistryE3SM.runDeviceBatch(d_tn, d_tt, None, d_tadv, d_state, d_photo, d_ext, t, dt, out, km,
+                                                    form=form, threads_per_sample=tps, stream=stream)
+        ms = timed(run)
+        key = form if form != "simplified" else f"simplified_{tps}"
+        forms[key] = {"value": B / (ms * 1e-3), "ms": ms}
+        results[key] = out[:nc].cpu().numpy()
+    best = max((k for k in forms if k.startswith("simplified")), key=lambda k: forms[k]["value"])
+    omega = torch.empty(B, m, dtype=torch.float64, device=dev)
+    ms_rates = timed(lambda: NetProductionRates.runDeviceBatch(d_state, d_photo, d_ext, omega, km, stream=stream))
+    rate_bytes = B * 8 * (3 + km.nSpec + photo.shape[1] + 2 * m)  # state row, photolysis, sources in; omega out
+    golden = np.load(E3SM_GOLDEN)[nc:, 6:6 + m]
+    acc = {}
+    for k, r in results.items():
+        y = r[:, 3:3 + m]
+        dmax = np.abs(y - golden)
+        i = np.unravel_index(int(dmax.argmax()), dmax.shape)
+        acc[k] = {"reference_criterion": float(dmax[i] / abs(golden[i])),
+                  "max_tolerance_units": float((dmax / (ATOL + RTOL * np.abs(golden))).max())}
+    # CPU restatement on the host cores (the E3SM leg's own CPU baseline), bounded sample
+    o = E3smOracle(km, native=True)
+    n = nc
+    t0 = time.perf_counter()
+    o.time_advance(tadv[:n], state[:n], photo[:n], ext[:n], TOL_NEWTON, tol_time)
+    el = time.perf_counter() - t0
+    n = int(min(B, max(nc, nc * round(cpu_seconds / max(el, 1e-6)))))
+    t0 = time.perf_counter()
+    o.time_advance(tadv[:n], state[:n], photo[:n], ext[:n], TOL_NEWTON, tol_time)
+    el = time.perf_counter() - t0
+    cores = os.cpu_count() or 1
+    return {"metric": METRIC, "value": forms[best]["value"], "unit": "samples/s", "form": best, "samples": B,
+            "workload": "reference uci_col E3SM scenario (53 active species, 106 reactions, 22 photolysis rates, "
+                        "external forcing), 80 columns tiled, 1800 s TR-BDF2",
+            "forms": forms,
+            "net_production_rates": {"value": B / (ms_rates * 1e-3), "unit": "samples/s", "ms": ms_rates,
+                                     "achieved_gbs": rate_bytes / (ms_rates * 1e-3) / 1e9,
+                                     "bytes_per_sample": rate_bytes // B},
+            "accuracy_vs_reference_golden": acc,
+            "cpu_baseline": {"value": n / el, "unit": "samples/s", "cores": cores, "kind": "port",
+                             "sample": f"first {n} samples, E3SM CPU restatement built for the host CPU, OpenMP over "
+                                       f"samples on {cores} threads ({el:.2f} s)"}}
+
+
 # ---- discrete adjoint -------------------------------------------------------------------------
 
 def adjoint_leg(km, state, tol_time, n: int, dev, stream) -> dict:
@@ -536,6 +639,9 @@ def engine_arm(args, world: int, rank: int, local: int):
 
     if rank == 0 and args.adjoint_samples > 0:
         line["adjoint"] = adjoint_leg(km, state, tol_time, args.adjoint_samples, dev, stream)
+
+    if rank == 0 and args.e3sm_samples > 0:
+        line["e3sm"] = e3sm_leg(args.e3sm_samples, min(args.cpu_seconds, 5.0), dev, stream)
 
     if not args.no_e2e:
         # end to end through the host-buffer C ABI: pinned host arrays in, results out, every copy
