@@ -40,6 +40,11 @@ class KineticModel {
     check(tchem_gb_mech_host_view(m_, &v), "tchem_gb_mech_host_view");
     return v;
   }
+  tchem_gb_e3sm_view e3sm_view() const {
+    tchem_gb_e3sm_view v{};
+    check(tchem_gb_mech_e3sm_view(m_, &v), "tchem_gb_mech_e3sm_view");
+    return v;
+  }
 
  private:
   tchem_gb_mech* m_ = nullptr;
@@ -134,6 +139,62 @@ struct AtmosphericChemistry {
     check(tchem_gb_time_advance_hostbuf(&h, 1, nullptr, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out,
                                         state_out, status, nullptr, &o, nullptr),
           "tchem_gb_time_advance_hostbuf");
+  }
+};
+
+// E3SM gas chemistry (TChem::AtmosphericChemistryE3SM, src/core/TChem_AtmosphericChemistryE3SM.hpp:47-104):
+// runDeviceBatch with the per-sample photo_rates[nbatch][n_photo] and external_sources[nbatch][m]
+// (either may be null). The rate constants are evaluated once per sample: [M], the adjust_reaction
+// and prod_O1D species must be constant species.
+struct AtmosphericChemistryE3SM {
+  static size_t getWorkSpaceSize(const KineticModel& kmcd, int nbatch, int form = TCHEM_GB_FORM_PLAIN_FP64) {
+    tchem_gb_advance_opts o{};
+    o.form = form;
+    const size_t n = tchem_gb_e3sm_workspace_bytes(kmcd.handle(), nbatch, &o);
+    if (n == 0) check(TCHEM_GB_ERR_ARG, "tchem_gb_e3sm_workspace_bytes");
+    return n;
+  }
+  static void runDeviceBatch(void* stream, const double* tol_newton, const double* tol_time, const double* fac,
+                             const tchem_gb_tadv* tadv, const double* state, const double* photo_rates, int n_photo,
+                             const double* external_sources, double* t_out, double* dt_out, double* state_out,
+                             const KineticModel& kmcd, int nbatch, int32_t* status,
+                             int form = TCHEM_GB_FORM_PLAIN_FP64, void* workspace = nullptr,
+                             size_t workspace_bytes = 0) {
+    tchem_gb_advance_opts o{};
+    o.form = form;
+    check(tchem_gb_e3sm_time_advance(kmcd.handle(), nbatch, tol_newton, tol_time, fac, tadv, state, photo_rates,
+                                     n_photo, external_sources, t_out, dt_out, state_out, status, nullptr, workspace,
+                                     workspace_bytes, &o, stream),
+          "tchem_gb_e3sm_time_advance");
+  }
+};
+
+// RHS-only batch APIs of the E3SM chemistry (src/core/TChem_ReactionRates.hpp:59-72,
+// src/core/TChem_RateofProgress.hpp:60-75, src/core/TChem_NetProductionRates.hpp:61-78); device
+// arrays: kfwd and rate_of_progress [nbatch][nReac], net_production_rates [nbatch][m].
+struct ReactionRates {
+  static void runDeviceBatch(void* stream, const double* state, double* kfwd, const KineticModel& kmcd, int nbatch,
+                             const double* photo_rates = nullptr, int n_photo = 0) {
+    check(tchem_gb_e3sm_reaction_rates(kmcd.handle(), nbatch, state, photo_rates, n_photo, kfwd, stream),
+          "tchem_gb_e3sm_reaction_rates");
+  }
+};
+
+struct RateofProgress {
+  static void runDeviceBatch(void* stream, const double* state, const double* photo_rates, int n_photo,
+                             double* rate_of_progress, const KineticModel& kmcd, int nbatch) {
+    check(tchem_gb_e3sm_rate_of_progress(kmcd.handle(), nbatch, state, photo_rates, n_photo, rate_of_progress, stream),
+          "tchem_gb_e3sm_rate_of_progress");
+  }
+};
+
+struct NetProductionRates {
+  static void runDeviceBatch(void* stream, const double* state, const double* photo_rates, int n_photo,
+                             const double* external_sources, double* net_production_rates, const KineticModel& kmcd,
+                             int nbatch) {
+    check(tchem_gb_e3sm_net_production_rates(kmcd.handle(), nbatch, state, photo_rates, n_photo, external_sources,
+                                             net_production_rates, stream),
+          "tchem_gb_e3sm_net_production_rates");
   }
 };
 

@@ -188,7 +188,13 @@ def test_cpp_shim_compiles_links_and_parses(tmp_path):
         "    tchem_gb::AtmosphericChemistry::adjointDeviceBatch(nullptr, nullptr, nullptr, nullptr, nullptr, km, 0,\n"
         "                                                       nullptr, nullptr, nullptr, 1, nullptr, nullptr, nullptr,\n"
         "                                                       nullptr);\n"
+        "    tchem_gb::AtmosphericChemistryE3SM::runDeviceBatch(nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,\n"
+        "                                                       nullptr, 0, nullptr, nullptr, nullptr, nullptr, km, 0,\n"
+        "                                                       nullptr);\n"
+        "    tchem_gb::NetProductionRates::runDeviceBatch(nullptr, nullptr, nullptr, 0, nullptr, nullptr, km, 0);\n"
         "  }\n"
+        "  tchem_gb_e3sm_view e = km.e3sm_view();\n"
+        '  std::printf("%d %d\\n", e.nJPL, e.nAdjust);\n'
         "  try { tchem_gb::KineticModel bad(\"/nonexistent.yaml\"); } catch (const std::logic_error&) { return 0; }\n"
         "  return 1;\n}\n")
     exe = tmp_path / "shim"
@@ -196,7 +202,9 @@ def test_cpp_shim_compiles_links_and_parses(tmp_path):
     r = subprocess.run([cxx, "-std=c++17", f"-I{ROOT / 'include'}", str(src), "-o", str(exe), f"-L{libdir}",
                         "-ltchem_gb", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    out = subprocess.run([str(exe), str(mech_path("cb05cl_ae5.yaml"))], capture_output=True, text=True)
+    out = subprocess.run([str(exe), str(mech_path("uci_v2_test3.yaml"))], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
-    km = KineticModel.from_file(mech_path("cb05cl_ae5.yaml"))
-    assert out.stdout.split() == [str(km.nSpec), str(km.nConstSpec), str(km.nReac)]
+    km = KineticModel.from_file(mech_path("uci_v2_test3.yaml"))
+    assert km.e3sm_view.nJPL == 10 and km.e3sm_view.nAdjust == 83  # the echo's adjustment pairs
+    assert out.stdout.split() == [str(km.nSpec), str(km.nConstSpec), str(km.nReac), str(km.e3sm_view.nJPL),
+                                  str(km.e3sm_view.nAdjust)]
