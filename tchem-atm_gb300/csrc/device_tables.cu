@@ -142,9 +142,19 @@ HostTables build_host_tables(const KineticModel& km) {
     p[0] = j.k0_A; p[1] = j.k0_B; p[2] = j.k0_C; p[3] = j.kinf_A; p[4] = j.kinf_B; p[5] = j.kinf_C; p[6] = j.Fc;
     p[7] = j.A; p[8] = j.B; p[9] = j.C;
   }
+  // Adjust factors grouped by reaction, file order kept within each reaction: applying them per
+  // reaction in parallel gives the products of the reference's serial pass, bit for bit.
+  {
+    std::vector<std::vector<int32_t>> per_r(R);
+    for (const auto& a : km.adjust_reaction) per_r[a.reaction_index].push_back(a.species_index);
+    ht.e3_adj_ptr.assign(R + 1, 0);
+    for (int r = 0; r < R; ++r) {
+      ht.e3_adj_ptr[r] = static_cast<int32_t>(ht.e3_adj_sp.size());
+      ht.e3_adj_sp.insert(ht.e3_adj_sp.end(), per_r[r].begin(), per_r[r].end());
+    }
+    ht.e3_adj_ptr[R] = static_cast<int32_t>(ht.e3_adj_sp.size());
+  }
   for (const auto& a : km.adjust_reaction) {
-    ht.e3_adj.push_back(a.reaction_index);
-    ht.e3_adj.push_back(a.species_index);
     if (a.species_index < m) {
       ht.e3sm_state_free = false;
       ht.e3sm_reason = "adjust_reaction of reaction " + std::to_string(a.reaction_index) + " names the active species " +
@@ -371,7 +381,8 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   const size_t o_rxn = sec(sizeof(int32_t) * ht.rx_n.size());
   const size_t o_e3t = sec(sizeof(int32_t) * R);
   const size_t o_e3p = sec(sizeof(double) * R * kE3smParams);
-  const size_t o_e3a = sec(sizeof(int32_t) * std::max<size_t>(1, ht.e3_adj.size()));
+  const size_t o_e3ap = sec(sizeof(int32_t) * (R + 1));
+  const size_t o_e3a = sec(sizeof(int32_t) * std::max<size_t>(1, ht.e3_adj_sp.size()));
   const size_t o_e3o = sec(sizeof(int32_t) * std::max<size_t>(1, ht.e3_o1d.size()));
   const size_t o_e3op = sec(sizeof(double) * std::max<size_t>(1, ht.e3_o1d_par.size()));
   std::vector<unsigned char> host(off, 0);
@@ -387,7 +398,9 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   std::memcpy(host.data() + o_rxn, ht.rx_n.data(), sizeof(int32_t) * ht.rx_n.size());
   std::memcpy(host.data() + o_e3t, ht.e3_type.data(), sizeof(int32_t) * R);
   std::memcpy(host.data() + o_e3p, ht.e3_param.data(), sizeof(double) * R * kE3smParams);
-  if (!ht.e3_adj.empty()) std::memcpy(host.data() + o_e3a, ht.e3_adj.data(), sizeof(int32_t) * ht.e3_adj.size());
+  std::memcpy(host.data() + o_e3ap, ht.e3_adj_ptr.data(), sizeof(int32_t) * (R + 1));
+  if (!ht.e3_adj_sp.empty())
+    std::memcpy(host.data() + o_e3a, ht.e3_adj_sp.data(), sizeof(int32_t) * ht.e3_adj_sp.size());
   if (!ht.e3_o1d.empty()) std::memcpy(host.data() + o_e3o, ht.e3_o1d.data(), sizeof(int32_t) * ht.e3_o1d.size());
   if (!ht.e3_o1d_par.empty())
     std::memcpy(host.data() + o_e3op, ht.e3_o1d_par.data(), sizeof(double) * ht.e3_o1d_par.size());
@@ -425,10 +438,10 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   t->dev.rx_S = ht.rx_S;
   t->dev.e3_type = reinterpret_cast<const int32_t*>(b + o_e3t);
   t->dev.e3_param = reinterpret_cast<const double*>(b + o_e3p);
-  t->dev.e3_adj = reinterpret_cast<const int32_t*>(b + o_e3a);
+  t->dev.e3_adj_ptr = reinterpret_cast<const int32_t*>(b + o_e3ap);
+  t->dev.e3_adj_sp = reinterpret_cast<const int32_t*>(b + o_e3a);
   t->dev.e3_o1d = reinterpret_cast<const int32_t*>(b + o_e3o);
   t->dev.e3_o1d_par = reinterpret_cast<const double*>(b + o_e3op);
-  t->dev.e3_nadj = static_cast<int32_t>(ht.e3_adj.size() / 2);
   t->dev.e3_no1d = static_cast<int32_t>(ht.e3_o1d.size() / 7);
   t->dev.M_index = ht.M_index;
   t->dev_x = t->dev;

@@ -71,10 +71,11 @@ struct MechDev {
   // JPL values then A, B, C.
   const int32_t* e3_type;     // [R] E3smRateType
   const double* e3_param;     // [R][kE3smParams]
-  const int32_t* e3_adj;      // [e3_nadj][2]: reaction, species (applied in this order)
+  const int32_t* e3_adj_ptr;  // [R+1] adjust factors of reaction r: e3_adj_sp[e3_adj_ptr[r] ..), file order
+  const int32_t* e3_adj_sp;   // species whose concentration multiplies the rate constant
   const int32_t* e3_o1d;      // [e3_no1d][7]: reactions 1..3, photolysis reaction, species 1..3
   const double* e3_o1d_par;   // [e3_no1d][6]: A1, C1, A2, C2, A3, C3
-  int32_t e3_nadj, e3_no1d, M_index;
+  int32_t e3_no1d, M_index;
 };
 
 // Host-side packed tables, built from a parsed kinetic model.
@@ -94,7 +95,7 @@ struct HostTables {
   std::string unsupported_reason;
   // E3SM tables (MechDev::e3_*); e3sm_state_free: no active species scales a rate constant, so
   // the E3SM time advance may evaluate them once per sample.
-  std::vector<int32_t> e3_type, e3_adj, e3_o1d;
+  std::vector<int32_t> e3_type, e3_adj_ptr, e3_adj_sp, e3_o1d;
   std::vector<double> e3_param, e3_o1d_par;
   int32_t M_index = -1;
   bool e3sm_valid = true;  // false: the tables cannot drive the E3SM kernels (reason below)

@@ -9,11 +9,13 @@
 // src/core/impl/TChem_Impl_ReactionRates.hpp:54-79; the net production rates start from the
 // external sources and scatter nu * q with atomics
 // (src/core/impl/TChem_Impl_NetProductionRates.hpp:52-112). Here one warp takes one sample: lanes
-// over reactions for the rate forms, lane 0 for the adjust pairs (they are applied serially in file
-// order, as the reference's Kokkos::single does, because two pairs may scale one reaction), and
-// the net production rates gather per species over the CSR program of the device tables (no
-// atomics; the reference's atomic order is unspecified). The work is a few hundred flops and
-// transcendentals per sample: these kernels are latency- and HBM-bound (state row in, one row out).
+// over reactions for the rate forms and their adjust factors (the reference applies the adjust
+// pairs serially in file order inside a Kokkos::single; grouped by reaction with that order kept,
+// each reaction's product is the same, bit for bit), lane 0 for the prod_O1D modifier, and the net
+// production rates gather per species over the CSR program of the device tables (no atomics; the
+// reference's atomic order is unspecified). Per sample the work is about two FP64 transcendentals
+// per reaction and a few hundred flops against about 1.7 KB in and out: on GB300 (FP64 about
+// 1.3 TFLOP/s) these kernels are bound by the FP64 pipe and latency, not by HBM.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -88,12 +90,13 @@ __global__ void __launch_bounds__(kE3smWarps * 32) e3sm_kernel(const __grid_cons
     const double* photo = P.photo ? P.photo + static_cast<size_t>(s) * P.n_photo : nullptr;
     for (int r = lane; r < R; r += 32) {
       const int type = M.e3_type[r];
-      kfor[r] = type != E3_NONE ? e3sm_rate(type, M.e3_param + kE3smParams * r, M.conv_exp[r], T, t_1, p, conv, mM)
-                                : ((photo && r < P.n_photo) ? photo[r] : 0.0);
+      double k = type != E3_NONE ? e3sm_rate(type, M.e3_param + kE3smParams * r, M.conv_exp[r], T, t_1, p, conv, mM)
+                                 : ((photo && r < P.n_photo) ? photo[r] : 0.0);
+      for (int a = M.e3_adj_ptr[r]; a < M.e3_adj_ptr[r + 1]; ++a) k *= x[M.e3_adj_sp[a]];  // adjust factors
+      kfor[r] = k;
     }
     __syncwarp();
-    if (lane == 0) {
-      for (int i = 0; i < M.e3_nadj; ++i) kfor[M.e3_adj[2 * i]] *= x[M.e3_adj[2 * i + 1]];
+    if (lane == 0) {  // the prod_O1D modifiers read one reaction's final rate and scale three others
       for (int i = 0; i < M.e3_no1d; ++i) {
         const int32_t* I = M.e3_o1d + 7 * i;
         const double* C = M.e3_o1d_par + 6 * i;
