@@ -19,6 +19,8 @@ from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
+
 from . import _capi
 from .atmospheric_chemistry import _opts, _ptr, _stream_ptr, _torch
 from .mechanism import KineticModel
@@ -67,6 +69,28 @@ class AtmosphericChemistryE3SM:
             _ptr(stats), ws_ptr, ws_bytes, C.byref(o), _stream_ptr(stream))
         _capi.check(rc, "tchem_gb_e3sm_time_advance")
         return status
+
+    @staticmethod
+    def runHostBatch(tol_newton, tol_time, tadv: np.ndarray, state: np.ndarray, photo_rates, external_sources,
+                     t_out: np.ndarray, kmcd: KineticModel, *, form: str | int = "plain", threads_per_sample: int = 0):
+        """Host-array variant (runHostBatch): copies in, advances on the GPU, copies out
+        (synchronous). Returns (state_out, t_out, dt_out, status) as numpy arrays."""
+        torch = _torch()
+        from .atmospheric_chemistry import tadv_to_device
+        dev = torch.device("cuda", torch.cuda.current_device())
+
+        def d(a):
+            return None if a is None or np.size(a) == 0 else torch.as_tensor(
+                np.ascontiguousarray(a, dtype=np.float64)).to(dev)
+        d_state = d(state)
+        out = d_state.clone()  # rows the advance does not write (skipped samples) come back unchanged
+        t = d(t_out)
+        dt = torch.zeros_like(t)
+        status = AtmosphericChemistryE3SM.runDeviceBatch(d(tol_newton), d(tol_time), None, tadv_to_device(tadv, dev),
+                                                         d_state, d(photo_rates), d(external_sources), t, dt, out,
+                                                         kmcd, form=form, threads_per_sample=threads_per_sample)
+        torch.cuda.synchronize(dev)
+        return out.cpu().numpy(), t.cpu().numpy(), dt.cpu().numpy(), status.cpu().numpy()
 
 
 class ReactionRates:

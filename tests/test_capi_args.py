@@ -53,3 +53,28 @@ def test_autotune_and_noalloc_reject_bad_arguments():
     assert f(None, 1, None, 4, *([None] * 10), None, None) == ERR_ARG
     handles = (C.c_void_p * 1)(km.handle.value)
     assert f(handles, 1, None, 0, *([None] * 10), None, None) == 0  # empty batch: nothing to do
+
+
+def test_e3sm_entry_points_reject_bad_arguments():
+    L = _capi.lib()
+    km = _km()
+    nul = C.c_void_p(0)
+    buf = C.c_void_p(1 << 20)  # never dereferenced: every call below returns before device work
+    for name in ("tchem_gb_e3sm_reaction_rates", "tchem_gb_e3sm_rate_of_progress"):
+        f = getattr(L, name)
+        assert f(km.handle, -1, buf, nul, 0, buf, nul) == ERR_ARG
+        assert f(km.handle, 4, buf, nul, 3, buf, nul) == ERR_ARG  # n_photo > 0 without photolysis rates
+        assert f(km.handle, 4, nul, nul, 0, buf, nul) == ERR_ARG and b"null" in L.tchem_gb_last_error()
+        assert f(None, 4, buf, nul, 0, buf, nul) == ERR_ARG
+        assert f(km.handle, 0, nul, nul, 0, nul, nul) == 0  # empty batch
+    f = L.tchem_gb_e3sm_net_production_rates
+    assert f(km.handle, 4, buf, nul, 0, nul, nul, nul) == ERR_ARG
+    assert f(km.handle, 4, buf, nul, -1, nul, buf, nul) == ERR_ARG
+    f = L.tchem_gb_e3sm_time_advance
+    o = _capi.AdvanceOpts()
+    assert f(km.handle, 4, *([nul] * 6), 0, nul, nul, nul, nul, nul, nul, nul, 0, C.byref(o), nul) == ERR_ARG
+    assert f(km.handle, 4, *([buf] * 5), nul, 2, nul, *([buf] * 4), nul, nul, 0, C.byref(o), nul) == ERR_ARG
+    assert f(None, 4, *([buf] * 6), 0, nul, *([buf] * 4), nul, nul, 0, C.byref(o), nul) == ERR_ARG
+    assert f(km.handle, 0, *([nul] * 6), 0, nul, nul, nul, nul, nul, nul, nul, 0, C.byref(o), nul) == 0
+    o.form = 9
+    assert f(km.handle, 4, *([buf] * 6), 0, nul, *([buf] * 4), nul, nul, 0, C.byref(o), nul) == ERR_ARG

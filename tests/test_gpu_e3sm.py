@@ -9,8 +9,9 @@ goldens and the CPU oracle:
   Newton and step decisions) within 5 units of the step tolerance of the oracle; every form passes
   the reference's own criterion against its golden (compareFilesValues <= 1e-8) and stays within
   10 tolerance units of it per species;
-* no photolysis input and no sources (NULL arrays) match the oracle; a mechanism whose rate
-  constants depend on an active species is refused.
+* no photolysis input and no sources (NULL arrays) match the oracle; samples already at t_end are
+  skipped with their rows kept, in place (state_out = state) and through the host-array variant;
+  a mechanism whose rate constants depend on an active species is refused.
 """
 from __future__ import annotations
 
@@ -167,3 +168,32 @@ reactions:
     tadv = time_advance_array(1, tend=1.0)
     with pytest.raises(TChemGBError, match="active species"):
         advance(km, state, None, None, tadv, np.tile([1e-12, 1e-6], (2, 1)), [1e-18, 1e-8], "plain")
+
+
+def test_skipped_samples_in_place_and_host_batch(uci_col_run):
+    """Samples with t_out >= t_end are skipped and keep their rows; state_out may be state (the
+    reference's E3SM driver advances in place); the host-array variant gives the same results."""
+    km, state, photo, ext, tadv, tol_time, tol_newton, *_ = uci_col_run
+    m = km.n_active
+    sel = slice(0, 16)
+    tadv = tadv[sel].copy()
+    tadv["tend"] = 60.0
+    t0 = np.zeros(16)
+    t0[::2] = 60.0  # every other sample is already at t_end
+    ref = E3smOracle(km).time_advance(tadv, state[sel], photo[sel], ext[sel], tol_newton, tol_time, t_out=t0)
+    d_state = dev(state[sel])
+    t = dev(t0)
+    dt = torch.zeros_like(t)
+    st = AtmosphericChemistryE3SM.runDeviceBatch(dev(tol_newton), dev(tol_time), None, tadv_to_device(tadv), d_state,
+                                                 dev(photo[sel]), dev(ext[sel]), t, dt, d_state, km)
+    torch.cuda.synchronize()
+    st = st.cpu().numpy()
+    out = d_state.cpu().numpy()
+    assert np.all(st[::2] == 2) and np.all(st[1::2] == 0) and np.all(ref[3] == st)
+    np.testing.assert_array_equal(out[::2], state[sel][::2])
+    assert rel_error(out[1::2, 3:3 + m], ref[0][1::2, 3:3 + m], tol_time[0, 0]).max() <= 1e-8
+    h_out, h_t, h_dt, h_st = AtmosphericChemistryE3SM.runHostBatch(tol_newton, tol_time, tadv, state[sel], photo[sel],
+                                                                   ext[sel], t0, km)
+    np.testing.assert_array_equal(h_st, st)
+    np.testing.assert_array_equal(h_out, out)
+    np.testing.assert_array_equal(h_t, t.cpu().numpy())
