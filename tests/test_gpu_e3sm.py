@@ -197,3 +197,18 @@ def test_skipped_samples_in_place_and_host_batch(uci_col_run):
     np.testing.assert_array_equal(h_st, st)
     np.testing.assert_array_equal(h_out, out)
     np.testing.assert_array_equal(h_t, t.cpu().numpy())
+
+
+@pytest.mark.parametrize("chem,inputfile,extra,golden", [
+    ("uci_v2.yaml", None, ["--batch_size=10", "--use_cloned_samples=true"], "net-production-rates.dat"),
+    ("uci_v2_test3.yaml", "uci_col_input_conditions.yaml", [], "uci_col_net_production_rates.dat")])
+def test_example_driver_writes_the_reference_output(tmp_path, chem, inputfile, extra, golden):
+    """The example driver, run with the reference gtest's options, writes the golden file."""
+    from tchem_gb.examples import net_production_rates as ex
+    out = tmp_path / "npr.dat"
+    args = [f"--chemfile={mech_path(chem)}", f"--outputfile={out}", f"--outputfile_times={tmp_path / 't.json'}",
+            "--verbose=true", *extra]
+    if inputfile:
+        args.append(f"--inputfile={E3 / inputfile}")
+    assert ex.main(args) == 0
+    assert out.read_text() == (E3 / golden).read_text()
