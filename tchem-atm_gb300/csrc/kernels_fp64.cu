@@ -245,26 +245,25 @@ __global__ void __launch_bounds__(kUnitWarps * 32) unit_kernel(const __grid_cons
       for (int e = T.pr_ptr[i]; e < T.pr_ptr[i + 1]; ++e) acc += T.pr_nu[e] * q[T.pr_r[e]];
       P.out[static_cast<size_t>(s) * m + i] = acc;
     }
-    return;
-  }
-  // Jacobian
-  for (int r = lane; r < L.R; r += 32) {
-    const int f0 = T.rf_ptr[r], f1 = T.rf_ptr[r + 1];
-    for (int f = f0; f < f1; ++f) {
-      double dv = keff[r];
-      for (int g = f0; g < f1; ++g)
-        if (g != f) dv *= x[T.rf_sp[g]];
-      d[f] = dv;
+  } else {  // Jacobian
+    for (int r = lane; r < L.R; r += 32) {
+      const int f0 = T.rf_ptr[r], f1 = T.rf_ptr[r + 1];
+      for (int f = f0; f < f1; ++f) {
+        double dv = keff[r];
+        for (int g = f0; g < f1; ++g)
+          if (g != f) dv *= x[T.rf_sp[g]];
+        d[f] = dv;
+      }
     }
-  }
-  double* J = P.out + static_cast<size_t>(s) * m * m;
-  for (int e = lane; e < m * m; e += 32) J[e] = 0.0;
-  __syncwarp();
-  for (int z = lane; z < L.NZ; z += 32) {
-    const int rc = T.jz_rc[z];
-    double acc = 0.0;
-    for (int e = T.jz_ptr[z]; e < T.jz_ptr[z + 1]; ++e) acc += T.jc_nu[e] * d[T.jc_f[e]];
-    J[static_cast<size_t>(rc >> 16) * m + (rc & 0xffff)] = acc;
+    double* J = P.out + static_cast<size_t>(s) * m * m;
+    for (int e = lane; e < m * m; e += 32) J[e] = 0.0;
+    __syncwarp();
+    for (int z = lane; z < L.NZ; z += 32) {
+      const int rc = T.jz_rc[z];
+      double acc = 0.0;
+      for (int e = T.jz_ptr[z]; e < T.jz_ptr[z + 1]; ++e) acc += T.jc_nu[e] * d[T.jc_f[e]];
+      J[static_cast<size_t>(rc >> 16) * m + (rc & 0xffff)] = acc;
+    }
   }
 }
 
