@@ -167,6 +167,40 @@ int tchem_gb_scenario_photolysis_rates(const char* yaml_path, int nbatch, double
 int tchem_gb_scenario_external_forcing(const char* yaml_path, const tchem_gb_mech* mech, int nbatch,
                                        double* ext_host, int* count);
 
+/* ---- Aerosol model (SIMPOL.1 gas-particle phase transfer) -----------------------------------
+ * TChem::AerosolModelData (src/core/TChem_AerosolModelData.hpp:30-80,
+ * src/core/TChem_AerosolModelData.cpp:60-303) over a parsed gas mechanism. The aerosol problem's
+ * ODE vector is [active gas species, particle 0's aerosol species, particle 1's, ...]
+ * (src/core/TChem_AerosolChemistry.cpp:116-131); its state row is [rho, p, T, active gas,
+ * constant gas, particles]. */
+typedef struct tchem_gb_aero tchem_gb_aero; /* opaque */
+typedef struct tchem_gb_aero_view {
+  int32_t nSpec;          /* aerosol species per particle */
+  int32_t nSpec_gas;      /* active gas species */
+  int32_t nConstSpec_gas; /* constant gas species */
+  int32_t nParticles;     /* computational particles */
+  int32_t nSimpol;        /* SIMPOL_PHASE_TRANSFER entries */
+  const double* molecular_weights; /* [nSpec] kg/mol */
+  const double* aerosol_density;   /* [nSpec] kg/m3 */
+  const double* aerosol_kappa;     /* [nSpec] */
+  const int32_t* simpol_index;     /* [nSimpol][3]: aerosol index in the ODE vector (particle 0), gas
+                                      index, compute_alpha (1: alpha from N star, 0: alpha = 0.1) */
+  const double* simpol_param;      /* [nSimpol][7]: B1, B2, B3, B4, diffusion coeff [m2/s], N star,
+                                      gas molecular weight [kg/mol] */
+} tchem_gb_aero_view;
+int tchem_gb_aero_create_from_file(const char* yaml_path, const tchem_gb_mech* gas, tchem_gb_aero** out);
+int tchem_gb_aero_create_from_string(const char* yaml_text, const tchem_gb_mech* gas, tchem_gb_aero** out);
+void tchem_gb_aero_destroy(tchem_gb_aero* aero);
+int tchem_gb_aero_host_view(const tchem_gb_aero* aero, tchem_gb_aero_view* view);
+/* AerosolModelData::setNumberofParticles (src/core/TChem_AerosolModelData.cpp:245-254). */
+int tchem_gb_aero_set_number_of_particles(tchem_gb_aero* aero, int n_particles);
+int tchem_gb_aero_species_name(const tchem_gb_aero* aero, int i, char* buf, int buflen);
+/* AerosolModelData::scenarioConditionParticles (src/core/TChem_AerosolModelData.cpp:256-300):
+ * num_conc[nbatch][nParticles] and the particle part of state rows of width dim (host arrays);
+ * *found = 0 when the file has no particles section (nothing written). */
+int tchem_gb_aero_scenario_particles(const char* yaml_path, const tchem_gb_aero* aero, int nbatch, double* num_conc,
+                                     double* state, int dim, int* found);
+
 /* Numerical form of the time advance. */
 enum tchem_gb_form {
   TCHEM_GB_FORM_PLAIN_FP64 = 0, /* FP64 Newton LU: the parity form */

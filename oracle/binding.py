@@ -46,6 +46,12 @@ def load(native: bool = False) -> C.CDLL:
         L.oracle_e3sm_net_production_rates.argtypes = [vp, vp, d, d, vp, vp, i, vp, vp]
         L.oracle_e3sm_time_advance.restype = i
         L.oracle_e3sm_time_advance.argtypes = [vp, vp, i, vp, vp, vp, vp, vp, i, vp, vp, vp, vp, vp, vp, i, i, i]
+        L.oracle_simpol_rhs.restype = i
+        L.oracle_simpol_rhs.argtypes = [vp, i, d, d, vp, vp, vp]
+        L.oracle_aerosol_rhs.restype = i
+        L.oracle_aerosol_rhs.argtypes = [vp, vp, d, d, vp, vp, vp, vp]
+        L.oracle_aerosol_time_advance.restype = i
+        L.oracle_aerosol_time_advance.argtypes = [vp, vp, i, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, i]
         _libs[native] = L
     return _libs[native]
 
@@ -172,6 +178,50 @@ class E3smOracle:
                                                int(bool(simplified)), int(nthreads))
         if rc != 0:
             raise RuntimeError(f"oracle_e3sm_time_advance returned {rc}")
+        return state_out, t_out, dt_out, status, stats
+
+
+class AerosolOracle:
+    """FP64 CPU restatement of the aerosol chemistry (gas RHS + SIMPOL.1 phase transfer) and its
+    TR-BDF2 advance, for a gas KineticModel and an AerosolModel (both outlive this object)."""
+
+    def __init__(self, gas, aero, native: bool = False):
+        self.gas, self.aero = gas, aero
+        self.lib = load(native)
+        self._km = C.cast(C.pointer(gas.view), C.c_void_p)
+        self._av = C.cast(C.pointer(aero.view), C.c_void_p)
+
+    def simpol_rhs(self, i_simpol: int, T, p, number_conc, x) -> np.ndarray:
+        x = _a(x)
+        out = np.zeros_like(x)
+        assert self.lib.oracle_simpol_rhs(self._av, int(i_simpol), float(T), float(p), _p(_a(number_conc)), _p(x),
+                                          _p(out)) == 0
+        return out
+
+    def rhs(self, T, p, number_conc, x, xconst) -> np.ndarray:
+        x = _a(x)
+        out = np.zeros_like(x)
+        xc = _a(xconst) if np.size(xconst) else None
+        assert self.lib.oracle_aerosol_rhs(self._km, self._av, float(T), float(p), _p(_a(number_conc)), _p(x), _p(xc),
+                                           _p(out)) == 0
+        return out
+
+    def time_advance(self, tadv, state, number_conc, tol_newton, tol_time, t_out=None, nthreads: int = 0):
+        """Returns (state_out, t_out, dt_out, status, stats) for state rows [rho, p, T, gas, particles]."""
+        B = state.shape[0]
+        state = _a(state)
+        state_out = state.copy()
+        t_out = np.array(tadv["tbeg"], dtype=np.float64) if t_out is None else np.array(t_out, dtype=np.float64)
+        dt_out = np.zeros(B)
+        status = np.zeros(B, dtype=np.int32)
+        from tchem_gb._capi import SAMPLE_STATS_DTYPE
+        stats = np.zeros(B, dtype=SAMPLE_STATS_DTYPE)
+        rc = self.lib.oracle_aerosol_time_advance(self._km, self._av, B, _p(_a(tol_newton)), _p(_a(tol_time)),
+                                                  _p(np.ascontiguousarray(tadv)), _p(state), _p(_a(number_conc)),
+                                                  _p(t_out), _p(dt_out), _p(state_out), _p(status), _p(stats),
+                                                  int(nthreads))
+        if rc != 0:
+            raise RuntimeError(f"oracle_aerosol_time_advance returned {rc}")
         return state_out, t_out, dt_out, status, stats
 
 

@@ -127,6 +127,65 @@ bool e3sm_kfor_depends_on_state(const tchem_gb_kmcd_view& km, const tchem_gb_e3s
   return false;
 }
 
+// --- SIMPOL.1 gas-particle phase transfer ----------------------------------------------------
+// src/core/impl/TChem_Impl_SIMPOL_constant.hpp:50-130 (accommodation coefficient, mean free path,
+// vapour pressure, kg/m3 -> ppm factor, partitioning constant),
+// src/core/impl/TChem_Impl_SingleParticleUtils.hpp:50-170 (particle volume, radius, mass and mean
+// molecular weight with the reference's floor values; Fuchs-Sutugin transition-regime rate),
+// src/core/impl/TChem_Impl_SIMPOL_phase_transfer.hpp:60-150 (condensation minus evaporation per
+// particle). Constants of src/core/TChem_Util.hpp: RUNIV 8.314472 J/mol/K, PI, ATMPA 101325 Pa.
+constexpr double kRuniv = 8.314472;
+constexpr double kPi = 3.141592653589793;
+constexpr double kAtmPa = 101325.0;
+constexpr long double kMinMass = 1.0e-25L;     // kg/m3
+constexpr long double kMinMw = 0.1L;           // kg/mol
+constexpr long double kMinDensity = 1800.0L;   // kg/m3
+
+// Adds SIMPOL entry i_simpol's transfer for particle i_part to omega (ODE vector x).
+void simpol_particle(const tchem_gb_aero_view& av, int i_simpol, int i_part, double t, double p,
+                     const double* number_conc, const double* x, double* omega) {
+  const int32_t* I = av.simpol_index + 3 * i_simpol;
+  const double* P = av.simpol_param + 7 * i_simpol;
+  const int aero = I[0], gas = I[1];
+  const double B1 = P[0], B2 = P[1], B3 = P[2], B4 = P[3], D = P[4], N_star = P[5], MW = P[6];
+  double alpha = 0.1;
+  if (I[2]) {
+    const double n23 = std::pow(N_star, 2.0 / 3.0);
+    double dh = -10.0 * (N_star - 1.0) + 7.53 * (n23 - 1.0) - 1.0;
+    double ds = -32.0 * (N_star - 1.0) + 9.21 * (n23 - 1.0) - 1.3;
+    dh = dh * 4184.0;
+    ds = ds * 4.184;
+    const double dg = dh - t * ds;
+    alpha = std::exp(-dg / (kRuniv * t));
+    alpha = alpha / (1.0 + alpha);
+  }
+  const double mfp = 3.0 * D / std::sqrt(8.0 * kRuniv * t / (kPi * MW));
+  double vp = B1 / t + B2 + B3 * t + B4 * std::log(t);
+  vp = kAtmPa * std::pow(10.0, vp);
+  const double kgm3_to_ppm = kRuniv / MW * 1.0e6 * t / p;
+  const double keq = vp / p / MW * 1.0e6;
+  const int first = av.nSpec_gas + i_part * av.nSpec;
+  double volume = static_cast<double>(kMinMass / kMinDensity);
+  double mass = static_cast<double>(kMinMass);
+  double moles = static_cast<double>(kMinMass / kMinMw);
+  for (int k = 0; k < av.nSpec; ++k) volume += x[first + k] / av.aerosol_density[k];
+  for (int k = 0; k < av.nSpec; ++k) {
+    mass += x[first + k];
+    moles += x[first + k] / av.molecular_weights[k];
+  }
+  const double radius = std::pow(volume * 3.0 / 4.0 / kPi, 1.0 / 3.0);
+  const double avg_mw = mass / moles;
+  const double kn = mfp / radius;
+  const double ffs = (0.75 * alpha * (1.0 + kn)) / (kn * kn + (1.0 + 0.283 * alpha) * kn + 0.75 * alpha);
+  double cond = 4.0 * kPi * radius * D * ffs;
+  double evap = cond * 1.0 * (keq * avg_mw / mass);
+  cond *= x[gas];
+  evap *= x[aero + i_part * av.nSpec];
+  const double diff = -evap + cond;
+  omega[gas] += -number_conc[i_part] * diff;
+  omega[aero + i_part * av.nSpec] += diff / kgm3_to_ppm;
+}
+
 // --- RHS: src/core/impl/TChem_Impl_ReactionRatesAerosol.hpp:57-143 --------------------------
 // concX[nSpec] (constant species last), kfor precomputed; omega[m]. src[m] (E3SM external
 // sources, src/core/impl/TChem_Impl_NetProductionRates.hpp:73-77) replaces the emissions.
@@ -289,6 +348,15 @@ struct Sample {
   // E3SM inputs: rate constants given per sample (kfor_in) and external sources (src) in place of
   // the emissions.
   const double* src = nullptr;
+  // Aerosol problem (src/core/problems/TChem_Impl_AerosolChemistry_Problem.hpp:70-160): the ODE
+  // vector is [active gas, particles]; the RHS is the gas RHS plus the SIMPOL transfers of every
+  // particle (src/core/impl/TChem_Impl_Aerosol_RHS.hpp:60-105); the Jacobian is a forward
+  // difference of it, as the reference's (computeJacobian -> computeNumericalJacobian).
+  const tchem_gb_aero_view* aero = nullptr;
+  const double* number_conc = nullptr;
+  double T_aero = 0.0, p_aero = 0.0;
+  int m_gas = 0;
+  std::vector<double> f0, fh, yh;
 
   Sample(const tchem_gb_kmcd_view& km_, double T, double p, const double* xconst, const double* k_scale = nullptr,
          const double* kfor_in = nullptr, const double* src_ = nullptr)
@@ -308,14 +376,55 @@ struct Sample {
     res.assign(m, 0.0);
     corr.assign(m, 0.0);
   }
-  void f(const double* y, double* out) {
-    std::copy(y, y + m, concX.begin());
+  // Switches this sample to the aerosol problem of av with number concentrations nc[nParticles].
+  void set_aerosol(const tchem_gb_aero_view* av, const double* nc, double T, double p) {
+    aero = av;
+    number_conc = nc;
+    T_aero = T;
+    p_aero = p;
+    m_gas = m;
+    m = av->nSpec_gas + av->nSpec * av->nParticles;
+    J.assign(static_cast<size_t>(m) * m, 0.0);
+    lu.resize(m);
+    res.assign(m, 0.0);
+    corr.assign(m, 0.0);
+    f0.assign(m, 0.0);
+    fh.assign(m, 0.0);
+    yh.assign(m, 0.0);
+  }
+  void aerosol_rhs(const double* y, double* out) {
+    std::copy(y, y + m_gas, concX.begin());
     reaction_rates(km, kfor.data(), concX.data(), out, rop.data(), src);
+    for (int i = m_gas; i < m; ++i) out[i] = 0.0;
+    for (int ip = 0; ip < aero->nParticles; ++ip)
+      for (int is = 0; is < aero->nSimpol; ++is) simpol_particle(*aero, is, ip, T_aero, p_aero, number_conc, y, out);
+  }
+  void f(const double* y, double* out) {
+    if (aero) {
+      aerosol_rhs(y, out);
+    } else {
+      std::copy(y, y + m, concX.begin());
+      reaction_rates(km, kfor.data(), concX.data(), out, rop.data(), src);
+    }
     ++st.n_rhs;
   }
   void jac(const double* y) {
-    std::copy(y, y + m, concX.begin());
-    jacobian(km, kfor.data(), concX.data(), J.data());
+    if (aero) {
+      // forward differences, column j with step 1e-8 max(|y_j|, 1e-20)
+      aerosol_rhs(y, f0.data());
+      std::copy(y, y + m, yh.begin());
+      for (int j = 0; j < m; ++j) {
+        const double h = 1e-8 * std::max(std::abs(y[j]), 1e-20);
+        yh[j] = y[j] + h;
+        aerosol_rhs(yh.data(), fh.data());
+        const double hh = yh[j] - y[j];
+        for (int i = 0; i < m; ++i) J[static_cast<size_t>(i) * m + j] = (fh[i] - f0[i]) / hh;
+        yh[j] = y[j];
+      }
+    } else {
+      std::copy(y, y + m, concX.begin());
+      jacobian(km, kfor.data(), concX.data(), J.data());
+    }
     ++st.n_jac;
   }
 
@@ -820,6 +929,74 @@ int oracle_e3sm_time_advance(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_v
   else
     run_batch<double>(kms, nullptr, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out, state_out, status, stats,
                       km->nSpec + 3, 0, simplified != 0, e3, photo, photo ? n_photo : 0, ext);
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(prev);
+#endif
+  return TCHEM_GB_OK;
+}
+
+int oracle_simpol_rhs(const tchem_gb_aero_view* av, int i_simpol, double T, double p, const double* number_conc,
+                      const double* x, double* omega) {
+  if (!av || !number_conc || !x || !omega || i_simpol < 0 || i_simpol >= av->nSimpol) return TCHEM_GB_ERR_ARG;
+  for (int ip = 0; ip < av->nParticles; ++ip) simpol_particle(*av, i_simpol, ip, T, p, number_conc, x, omega);
+  return TCHEM_GB_OK;
+}
+
+int oracle_aerosol_rhs(const tchem_gb_kmcd_view* km, const tchem_gb_aero_view* av, double T, double p,
+                       const double* number_conc, const double* x, const double* xconst, double* omega) {
+  if (!km || !av || !number_conc || !x || !omega || (km->nConstSpec > 0 && !xconst)) return TCHEM_GB_ERR_ARG;
+  Sample<double> smp(*km, T, p, xconst);
+  smp.set_aerosol(av, number_conc, T, p);
+  smp.f(x, omega);
+  return TCHEM_GB_OK;
+}
+
+int oracle_aerosol_time_advance(const tchem_gb_kmcd_view* km, const tchem_gb_aero_view* av, int nbatch,
+                                const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
+                                const double* state, const double* number_conc, double* t_out, double* dt_out,
+                                double* state_out, int32_t* status, tchem_gb_sample_stats* stats, int nthreads) {
+  if (!km || !av || nbatch < 0 || !tol_newton || !tol_time || !tadv || !state || !number_conc || !t_out || !dt_out ||
+      !state_out || av->nParticles < 1)
+    return TCHEM_GB_ERR_ARG;
+  const int n = km->nSpec, mg = n - km->nConstSpec;
+  const int npart = av->nParticles * av->nSpec;
+  const int dim = 3 + n + npart;
+#ifdef _OPENMP
+  const int prev = omp_get_max_threads();
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#endif
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int b = 0; b < nbatch; ++b) {
+    const tchem_gb_tadv& ta = tadv[b];
+    if (stats) stats[b] = tchem_gb_sample_stats{};
+    if (t_out[b] >= ta.tend) {
+      if (status) status[b] = TCHEM_GB_SAMPLE_SKIPPED;
+      continue;
+    }
+    const double* row = state + static_cast<size_t>(b) * dim;
+    double* out = state_out + static_cast<size_t>(b) * dim;
+    const double p = row[1], T = row[2];
+    // ODE vector [active gas, particles]; the constant gas species sit between them in the row
+    std::vector<double> y(mg + npart);
+    std::copy(row + 3, row + 3 + mg, y.begin());
+    std::copy(row + 3 + n, row + 3 + n + npart, y.begin() + mg);
+    Sample<double> smp(*km, T, p, row + 3 + mg);
+    smp.set_aerosol(av, number_conc + static_cast<size_t>(b) * av->nParticles, T, p);
+    Settings s{ta.max_num_newton_iterations, std::max(1, ta.jacobian_interval), ta.num_time_iterations_per_interval,
+               0, false, tol_newton[0], tol_newton[1], tol_time};
+    double to = 0.0, dto = 0.0;
+    const int st = smp.integrate(y.data(), ta.tbeg, ta.tend, ta.dt, ta.dtmin, ta.dtmax, s, to, dto);
+    if (status) status[b] = st;
+    if (stats) stats[b] = smp.st;
+    if (st == TCHEM_GB_SAMPLE_NEGATIVE_DT) continue;
+    // src/core/TChem_AerosolChemistry.cpp:168-172: active gas and particles back, T; rho, p and the
+    // constant species are left as they are (copied through here)
+    std::copy(row, row + dim, out);
+    std::copy(y.begin(), y.begin() + mg, out + 3);
+    std::copy(y.begin() + mg, y.end(), out + 3 + n);
+    t_out[b] = to;
+    dt_out[b] = dto;
+  }
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(prev);
 #endif

@@ -85,6 +85,28 @@ int oracle_e3sm_time_advance(const tchem_gb_kmcd_view* km, const tchem_gb_e3sm_v
                              double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats,
                              int lu_fp32, int simplified, int nthreads);
 
+/* Aerosol chemistry with SIMPOL.1 gas-particle phase transfer (TChem::AerosolChemistry), ODE
+ * vector x = [active gas species, particle 0's aerosol species, ...]:
+ *   oracle_simpol_rhs     adds entry i_simpol's transfer for every particle to omega
+ *                         (src/core/impl/TChem_Impl_SIMPOL_phase_transfer.hpp:60-150 with
+ *                         TChem_Impl_SIMPOL_constant.hpp:50-130 and
+ *                         TChem_Impl_SingleParticleUtils.hpp:50-170)
+ *   oracle_aerosol_rhs    omega = gas RHS (box model, rate constants of KForwardAerosol) + every
+ *                         particle's SIMPOL transfers (src/core/impl/TChem_Impl_Aerosol_RHS.hpp:60-105);
+ *                         xconst = constant gas species
+ *   oracle_aerosol_time_advance  the TR-BDF2 advance of the aerosol problem on state rows
+ *                         [rho, p, T, active gas, constant gas, particles] with number_conc[nbatch][nParticles]
+ *                         (src/core/TChem_AerosolChemistry.cpp:55-172), forward-difference Jacobian as
+ *                         the reference's AerosolChemistry_Problem; tol_time[m_ode][2]. */
+int oracle_simpol_rhs(const tchem_gb_aero_view* av, int i_simpol, double T, double p, const double* number_conc,
+                      const double* x, double* omega);
+int oracle_aerosol_rhs(const tchem_gb_kmcd_view* km, const tchem_gb_aero_view* av, double T, double p,
+                       const double* number_conc, const double* x, const double* xconst, double* omega);
+int oracle_aerosol_time_advance(const tchem_gb_kmcd_view* km, const tchem_gb_aero_view* av, int nbatch,
+                                const double* tol_newton, const double* tol_time, const tchem_gb_tadv* tadv,
+                                const double* state, const double* number_conc, double* t_out, double* dt_out,
+                                double* state_out, int32_t* status, tchem_gb_sample_stats* stats, int nthreads);
+
 /* Discrete adjoint of the plain form on a recorded step sequence (the engine's
  * tchem_gb_time_advance_record / tchem_gb_adjoint), restated densely on the CPU, one mechanism:
  *   oracle_time_advance_record: oracle_time_advance (FP64) recording the accepted step sizes

@@ -51,6 +51,15 @@ class E3smView(C.Structure):
     ]
 
 
+class AeroView(C.Structure):
+    _fields_ = [
+        ("nSpec", C.c_int32), ("nSpec_gas", C.c_int32), ("nConstSpec_gas", C.c_int32), ("nParticles", C.c_int32),
+        ("nSimpol", C.c_int32), ("molecular_weights", C.POINTER(C.c_double)),
+        ("aerosol_density", C.POINTER(C.c_double)), ("aerosol_kappa", C.POINTER(C.c_double)),
+        ("simpol_index", C.POINTER(C.c_int32)), ("simpol_param", C.POINTER(C.c_double)),
+    ]
+
+
 class AdvanceOpts(C.Structure):
     _fields_ = [("form", C.c_int32), ("threads_per_sample", C.c_int32), ("reserved", C.c_int32 * 6)]
 
@@ -89,6 +98,14 @@ def lib() -> C.CDLL:
         "tchem_gb_mech_e3sm_view": (C.c_int, [vp, C.POINTER(E3smView)]),
         "tchem_gb_scenario_photolysis_rates": (C.c_int, [C.c_char_p, C.c_int, vp, C.POINTER(C.c_int)]),
         "tchem_gb_scenario_external_forcing": (C.c_int, [C.c_char_p, vp, C.c_int, vp, C.POINTER(C.c_int)]),
+        "tchem_gb_aero_create_from_file": (C.c_int, [C.c_char_p, vp, C.POINTER(vp)]),
+        "tchem_gb_aero_create_from_string": (C.c_int, [C.c_char_p, vp, C.POINTER(vp)]),
+        "tchem_gb_aero_destroy": (None, [vp]),
+        "tchem_gb_aero_host_view": (C.c_int, [vp, C.POINTER(AeroView)]),
+        "tchem_gb_aero_set_number_of_particles": (C.c_int, [vp, C.c_int]),
+        "tchem_gb_aero_species_name": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int]),
+        "tchem_gb_aero_scenario_particles": (C.c_int, [C.c_char_p, vp, C.c_int, vp, vp, C.c_int,
+                                                       C.POINTER(C.c_int)]),
     }
     popts = C.POINTER(AdvanceOpts)
     optional = {

@@ -14,7 +14,11 @@ Everything copied is data the reference's own tests and examples use:
     net-production-rate files (src/unit-tests/references/{reaction_rates,rate_of_progress,
     net_production_rates}/*.dat, compared as text), the 80-column uci scenario they and the E3SM
     time advance read (photolysis rates and external forcing included), and that time advance's
-    end states (src/unit-tests/references/atmospheric_chemistry_e3sm/uci_col/full_gas.dat).
+    end states (src/unit-tests/references/atmospheric_chemistry_e3sm/uci_col/full_gas.dat),
+  * the aerosol (SIMPOL.1 phase transfer) inputs and goldens: the Simpol and CB05CL_AE5_w_simpolSOA
+    example files, the SIMPOL RHS golden (src/unit-tests/references/partmc_integration/simpol/),
+    the TR-BDF2 goldens src/unit-tests/TinesODE/references/*.hdf5 (decoded at their raw data
+    offset) and the CAMP SIMPOL trajectory.
 Run settings of each case come from the reference's scripts and are recorded in manifest.json.
 """
 from __future__ import annotations
@@ -91,6 +95,26 @@ def main(ref: Path) -> None:
                              skip_header=1)
     np.save(e3sm_dir / "uci_col_full_gas.npy", full_gas)
 
+    aero_dir = HERE / "aerosol"
+    aero_dir.mkdir(exist_ok=True)
+    aero_copies = {
+        "simpol_config_gas.yaml": f"{RUNS}/Simpol/config_gas.yaml",
+        "simpol_phase_transfer.yaml": f"{RUNS}/Simpol/test_SIMPOL_phase_transfer.yaml",
+        "simpol_scenario_particles.yaml": f"{RUNS}/Simpol/scenario_conditions_particle.yaml",
+        "cb05_soa_config_full_gas.yaml": f"{RUNS}/CB05CL_AE5_w_simpolSOA/config_full_gas.yaml",
+        "cb05_soa_mechanism_aero.yaml": f"{RUNS}/CB05CL_AE5_w_simpolSOA/mechanism_aero.yaml",
+        "cb05_soa_scenario_particles.yaml": f"{RUNS}/CB05CL_AE5_w_simpolSOA/scenario_conditions_particle.yaml",
+        "Simpol_RHS_HOST.txt": "src/unit-tests/references/partmc_integration/simpol/Simpol_RHS_HOST.txt",
+    }
+    for dst, src in aero_copies.items():
+        shutil.copyfile(ref / src, aero_dir / dst)
+    for name in ("full_gas", "batched_full_gas", "batched_cb_full_gas"):
+        raw = (ref / f"src/unit-tests/TinesODE/references/{name}.hdf5").read_bytes()
+        n = (len(raw) - 2048) // 8  # one dataset of little-endian doubles at byte 2048
+        np.save(aero_dir / f"tines_{name}.npy", np.frombuffer(raw[2048:2048 + 8 * n], dtype="<f8"))
+    np.save(aero_dir / "camp_simpol.npy",
+            np.loadtxt(ref / RUNS / "Simpol" / "camp_out" / "SIMPOL_phase_transfer_results.txt"))
+
     manifest = {
         "cb05cl_ae5_full_gas": {
             "source": "src/unit-tests/CB05CL_AE5/references/full_gas.hdf5",
@@ -112,6 +136,33 @@ def main(ref: Path) -> None:
                         "settings": {"tend": 100, "dtmin": 1e-20, "dtmax": 0.1, "output_every": 1.0}}
                  for name, (src, rt) in camp.items()},
         "echo": {dst: src for dst, src in echoes.items()},
+        "aerosol": {
+            "files": {f"aerosol/{dst}": src for dst, src in aero_copies.items()},
+            "Simpol_RHS_HOST.txt": {"run": "src/unit-tests/TChem_Test_Simpol_RHS.hpp:60-140",
+                                    "inputs": {"T": 272.5, "p": 101253.3, "number_conc": 1.3e6, "ethanol": 0.1,
+                                               "ethanol_aq": 1.0e-8, "H2O_aq": 1.4e-2},
+                                    "criterion": "compareFilesValues <= 1e-12 on the written text"},
+            "tines": {
+                "source": "src/unit-tests/TinesODE/references/{full_gas,batched_full_gas,batched_cb_full_gas}.hdf5",
+                "run": "src/unit-tests/TinesODE/CMakeLists.txt",
+                "decode": "one dataset of doubles at byte 2048; rows (iter, t, dt, rho, p, T, species...), "
+                          "all samples of an iteration in a row block",
+                "settings": {"tend": 600, "dt_in": 1e-20, "dtmin": 1e-20, "dtmax": 10, "iters_per_interval": 10,
+                             "max_intervals": 2, "atol_newton": 1e-18, "rtol_newton": 1e-8, "max_newton": 100,
+                             "atol_time": 1e-12, "rtol_time": 1e-4, "jacobian_interval": 1},
+                "cases": {"tines_full_gas.npy": {"gas": "simpol_config_gas.yaml", "aero": "simpol_phase_transfer.yaml",
+                                                 "particles": "simpol_scenario_particles.yaml", "batch": 1},
+                          "tines_batched_full_gas.npy": {"gas": "simpol_config_gas.yaml",
+                                                         "aero": "simpol_phase_transfer.yaml",
+                                                         "particles": "simpol_scenario_particles.yaml", "batch": 3},
+                          "tines_batched_cb_full_gas.npy": {"gas": "cb05_soa_config_full_gas.yaml",
+                                                            "aero": "cb05_soa_mechanism_aero.yaml",
+                                                            "particles": "cb05_soa_scenario_particles.yaml",
+                                                            "batch": 3}},
+                "criterion": "compare_tchem.py norm-relative L1/L2/Linf <= 1e-8"},
+            "camp_simpol.npy": {"source": f"{RUNS}/Simpol/camp_out/SIMPOL_phase_transfer_results.txt",
+                                "columns": "time [s], then ethanol, ethanol_aq, H2O_aq as pairs of CAMP columns"},
+        },
         "e3sm": {
             "files": {f"e3sm/{dst}": src for dst, src in e3sm_copies.items()},
             "reaction-rates.dat": {"run": "src/unit-tests/TChem_Test_ReactionRates.hpp:28-50",
