@@ -50,6 +50,37 @@ class KineticModel {
   tchem_gb_mech* m_ = nullptr;
 };
 
+// Owning handle of a parsed aerosol model (TChem::AerosolModelData over a gas KineticModel, which
+// must outlive it).
+class AerosolModel {
+ public:
+  AerosolModel(const std::string& yaml_path, const KineticModel& gas) {
+    check(tchem_gb_aero_create_from_file(yaml_path.c_str(), gas.handle(), &a_), "tchem_gb_aero_create_from_file");
+  }
+  ~AerosolModel() { tchem_gb_aero_destroy(a_); }
+  AerosolModel(const AerosolModel&) = delete;
+  AerosolModel& operator=(const AerosolModel&) = delete;
+  const tchem_gb_aero* handle() const { return a_; }
+  tchem_gb_aero_view view() const {
+    tchem_gb_aero_view v{};
+    check(tchem_gb_aero_host_view(a_, &v), "tchem_gb_aero_host_view");
+    return v;
+  }
+  void setNumberofParticles(int n) { check(tchem_gb_aero_set_number_of_particles(a_, n), "tchem_gb_aero_set_number_of_particles"); }
+  // scenarioConditionParticles: num_conc[nbatch][nParticles] and the particle part of state rows
+  // of width dim (host arrays); false when the file has no particles section.
+  bool scenarioConditionParticles(const std::string& yaml_path, int nbatch, double* num_conc, double* state,
+                                  int dim) const {
+    int found = 0;
+    check(tchem_gb_aero_scenario_particles(yaml_path.c_str(), a_, nbatch, num_conc, state, dim, &found),
+          "tchem_gb_aero_scenario_particles");
+    return found != 0;
+  }
+
+ private:
+  tchem_gb_aero* a_ = nullptr;
+};
+
 struct AtmosphericChemistry {
   // getWorkSpaceSize(kmcd) for a batch of nbatch samples, in bytes of device memory.
   static size_t getWorkSpaceSize(const KineticModel& kmcd, int nbatch, int form = TCHEM_GB_FORM_PLAIN_FP64) {

@@ -182,7 +182,7 @@ def test_cpp_shim_compiles_links_and_parses(tmp_path):
         "  tchem_gb::KineticModel km(argv[1]);\n"
         "  tchem_gb_kmcd_view v = km.view();\n"
         '  std::printf("%d %d %d\\n", v.nSpec, v.nConstSpec, v.nReac);\n'
-        "  if (argc > 2) {  // referenced, not run: the device entry points of the C++ face link\n"
+        "  if (argc > 4) {  // referenced, not run: the device entry points of the C++ face link\n"
         "    tchem_gb::AtmosphericChemistry::autotune(nullptr, km, 2, 0, nullptr, nullptr, nullptr, nullptr, nullptr,\n"
         "                                             nullptr, nullptr, nullptr);\n"
         "    tchem_gb::AtmosphericChemistry::adjointDeviceBatch(nullptr, nullptr, nullptr, nullptr, nullptr, km, 0,\n"
@@ -192,6 +192,10 @@ def test_cpp_shim_compiles_links_and_parses(tmp_path):
         "                                                       nullptr, 0, nullptr, nullptr, nullptr, nullptr, km, 0,\n"
         "                                                       nullptr);\n"
         "    tchem_gb::NetProductionRates::runDeviceBatch(nullptr, nullptr, nullptr, 0, nullptr, nullptr, km, 0);\n"
+        "  }\n"
+        "  if (argc > 3) {  // an aerosol model over this gas mechanism\n"
+        "    tchem_gb::AerosolModel am(argv[3], km);\n"
+        '    std::printf("aero %d %d\\n", am.view().nSpec, am.view().nSimpol);\n'
         "  }\n"
         "  tchem_gb_e3sm_view e = km.e3sm_view();\n"
         '  std::printf("%d %d\\n", e.nJPL, e.nAdjust);\n'
@@ -206,5 +210,10 @@ def test_cpp_shim_compiles_links_and_parses(tmp_path):
     assert out.returncode == 0, out.stderr
     km = KineticModel.from_file(mech_path("uci_v2_test3.yaml"))
     assert km.e3sm_view.nJPL == 10 and km.e3sm_view.nAdjust == 83  # the echo's adjustment pairs
+    aero_dir = mech_path("x").parent.parent / "aerosol"
+    out_a = subprocess.run([str(exe), str(aero_dir / "simpol_config_gas.yaml"), "0", str(aero_dir / "simpol_phase_transfer.yaml")],
+                           capture_output=True, text=True)
+    assert out_a.returncode == 0, out_a.stderr
+    assert "aero 2 1" in out_a.stdout
     assert out.stdout.split() == [str(km.nSpec), str(km.nConstSpec), str(km.nReac), str(km.e3sm_view.nJPL),
                                   str(km.e3sm_view.nAdjust)]
