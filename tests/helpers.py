@@ -56,9 +56,16 @@ def host_time_loop(advance, state: np.ndarray, tadv: np.ndarray, tend: float, ma
     return np.array(rows), state
 
 
+def printed(x) -> np.ndarray:
+    """Values as the reference's example drivers write them (%15.10e) and read back."""
+    return np.vectorize(lambda v: float(f"{v:15.10e}"))(np.asarray(x, dtype=np.float64))
+
+
 def compare_files_values(test: np.ndarray, ref: np.ndarray) -> float:
-    """The criterion of TChem::Test::compareFilesValues (src/core/TChem_Util.hpp:1130-1180): the
-    relative error |test - ref| / ref at the element with the largest absolute difference."""
+    """The criterion of TChem::Test::compareFilesValues (src/core/TChem_Util.hpp:1130-1180) on two
+    written files: the relative error |test - ref| / ref at the element with the largest absolute
+    difference. Pass both as written (printed()); comparing full-precision values with printed ones
+    instead measures the printing rounding of the largest values."""
     d = np.abs(np.asarray(test, dtype=np.float64) - np.asarray(ref, dtype=np.float64))
     i = np.unravel_index(int(d.argmax()), d.shape)
     return float(d[i] / abs(ref[i])) if d[i] > 0 else 0.0
