@@ -20,6 +20,8 @@ def load(native: bool = False) -> C.CDLL:
             build(native=native)
         L = C.CDLL(str(path))
         vp = C.c_void_p
+        L.oracle_set_lu_tile_bits.restype = C.c_int
+        L.oracle_set_lu_tile_bits.argtypes = [C.c_int]
         L.oracle_kforward.restype = C.c_int
         L.oracle_kforward.argtypes = [vp, C.c_double, C.c_double, vp]
         L.oracle_reaction_rates.restype = C.c_int

@@ -4,6 +4,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <limits>
 #include <vector>
@@ -252,6 +253,24 @@ void jacobian(const tchem_gb_kmcd_view& km, const double* kfor, const double* co
   }
 }
 
+// Mantissa bits kept in the operands of the blocked trailing update of FP32 factorizations
+// (oracle_set_lu_tile_bits): 0 = unblocked FP32 LU; 10 = TF32 tiles, 7 = BF16 tiles.
+int g_lu_tile_bits = 0;
+
+// Round-to-nearest-even of an FP32 value to `keep` mantissa bits (TF32: 10, BF16: 7).
+float round_mantissa(float x, int keep) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7f800000u) == 0x7f800000u) return x;  // inf, nan
+  const int drop = 23 - keep;
+  const uint32_t lsb = (u >> drop) & 1u;
+  u += (1u << (drop - 1)) - 1u + lsb;
+  u &= ~((1u << drop) - 1u);
+  float y;
+  std::memcpy(&y, &u, 4);
+  return y;
+}
+
 // --- dense LU with partial pivoting (row swaps; first maximum in the current row order) ---
 template <typename T>
 struct DenseLU {
@@ -265,11 +284,54 @@ struct DenseLU {
     piv.assign(n, 0);
     w.assign(n, T(0));
   }
+  // Blocked right-looking LU as a tensor-core factorization computes it: 32-column panels factored
+  // with partial pivoting in FP32, U12 = L11^-1 A12 in FP32, and the trailing update
+  // A22 -= L21 U12 with both operands rounded to `keep` mantissa bits and FP32 accumulation of each
+  // panel's 32 products.
+  bool factor_blocked(int keep) {
+    const int NB = 32;
+    for (int p0 = 0; p0 < n; p0 += NB) {
+      const int p1 = std::min(n, p0 + NB);
+      for (int k = p0; k < p1; ++k) {
+        int p = k;
+        T amax = std::abs(a[static_cast<size_t>(k) * n + k]);
+        for (int i = k + 1; i < n; ++i) {
+          const T v = std::abs(a[static_cast<size_t>(i) * n + k]);
+          if (v > amax) { amax = v; p = i; }
+        }
+        if (!(amax > T(0)) || !std::isfinite(static_cast<double>(amax))) return false;
+        piv[k] = p;
+        if (p != k)
+          for (int j = 0; j < n; ++j) std::swap(a[static_cast<size_t>(k) * n + j], a[static_cast<size_t>(p) * n + j]);
+        const T inv = T(1) / a[static_cast<size_t>(k) * n + k];
+        for (int i = k + 1; i < n; ++i) {
+          const T l = a[static_cast<size_t>(i) * n + k] * inv;
+          a[static_cast<size_t>(i) * n + k] = l;
+          for (int j = k + 1; j < p1; ++j) a[static_cast<size_t>(i) * n + j] -= l * a[static_cast<size_t>(k) * n + j];
+        }
+      }
+      for (int k = p0; k < p1; ++k)
+        for (int i = k + 1; i < p1; ++i) {
+          const T l = a[static_cast<size_t>(i) * n + k];
+          for (int j = p1; j < n; ++j) a[static_cast<size_t>(i) * n + j] -= l * a[static_cast<size_t>(k) * n + j];
+        }
+      for (int i = p1; i < n; ++i)
+        for (int j = p1; j < n; ++j) {
+          float acc = 0.f;
+          for (int k = p0; k < p1; ++k)
+            acc += round_mantissa(static_cast<float>(a[static_cast<size_t>(i) * n + k]), keep) *
+                   round_mantissa(static_cast<float>(a[static_cast<size_t>(k) * n + j]), keep);
+          a[static_cast<size_t>(i) * n + j] -= acc;
+        }
+    }
+    return true;
+  }
   // A = I - c J, built in double and rounded to T.
   bool factor(const double* J, double c) {
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j)
         a[static_cast<size_t>(i) * n + j] = static_cast<T>((i == j ? 1.0 : 0.0) - c * J[static_cast<size_t>(i) * n + j]);
+    if (sizeof(T) == 4 && g_lu_tile_bits > 0) return factor_blocked(g_lu_tile_bits);
     for (int k = 0; k < n; ++k) {
       int p = k;
       T amax = std::abs(a[static_cast<size_t>(k) * n + k]);
@@ -830,6 +892,12 @@ Settings replay_settings(const tchem_gb_tadv& ta, const double* tol_newton) {
 }  // namespace
 
 extern "C" {
+
+int oracle_set_lu_tile_bits(int bits) {
+  if (bits != 0 && (bits < 1 || bits > 23)) return TCHEM_GB_ERR_ARG;
+  g_lu_tile_bits = bits;
+  return TCHEM_GB_OK;
+}
 
 int oracle_kforward(const tchem_gb_kmcd_view* km, double T, double p, double* kfor) {
   if (!km || !kfor) return TCHEM_GB_ERR_ARG;

@@ -33,6 +33,11 @@
 extern "C" {
 #endif
 
+/* FP32 factorizations (lu_fp32 >= 1 below) as a tensor-core factorization computes them: 32-column
+ * panels in FP32 and the trailing update with operands rounded to `bits` mantissa bits (10: TF32,
+ * 7: BF16) and FP32 accumulation; 0 (default): the unblocked FP32 LU. A process-wide setting. */
+int oracle_set_lu_tile_bits(int bits);
+
 /* kfor[nReac] for one (T, p). */
 int oracle_kforward(const tchem_gb_kmcd_view* km, double T, double p, double* kfor);
 /* omega[m] = d x_active / dt for x[nSpec] (constant species last). */
