@@ -375,6 +375,43 @@ int tchem_gb_e3sm_time_advance(const tchem_gb_mech* mech, int nbatch, const doub
                                int32_t* status, tchem_gb_sample_stats* stats, void* workspace,
                                size_t workspace_bytes, const tchem_gb_advance_opts* opts, void* stream);
 
+/* ---- Gas-aerosol chemistry (SIMPOL.1 phase transfer): time advance and RHS --------------------
+ * TChem::AerosolChemistry::runDeviceBatch (src/core/TChem_AerosolChemistry.hpp:87-103,
+ * src/core/TChem_AerosolChemistry.cpp:30-172, 236-260): TR-BDF2 on the ODE vector [active gas,
+ * particle 0's aerosol species, particle 1's, ...] of M = m + nParticles * nSpec entries, with one
+ * gas mechanism (box-model rate forms) and one aerosol model per call; plain FP64 form, one warp
+ * per sample, device arrays, stream-ordered.
+ *   tol_time[M][2]; number_conc[nbatch][nParticles]; state and state_out rows [rho, p, T, active
+ *   gas, constant gas, particles] of width 3 + nSpec + nParticles * nSpec_aerosol (may alias).
+ * The Newton Jacobian is a forward difference of the RHS, column j with the step
+ * 1e-8 max(|y_j|, 1e-20) (the reference's computeJacobian); fac, the reference's per-sample
+ * difference factors, may be NULL and is not read. rho, p, T and the constant gas species are
+ * copied through. Refused with TCHEM_GB_ERR_UNSUPPORTED: a SIMPOL entry whose gas species is a
+ * constant species, M above 320, or rate forms outside the box model's. The workspace holds the
+ * work queue, the device error word (tchem_gb_device_error) and, for large M, the Newton
+ * matrices: tchem_gb_aero_workspace_bytes (NULL workspace: library-owned). */
+size_t tchem_gb_aero_workspace_bytes(const tchem_gb_mech* mech, const tchem_gb_aero* aero, int nbatch);
+int tchem_gb_aero_time_advance(const tchem_gb_mech* mech, const tchem_gb_aero* aero, int nbatch,
+                               const double* tol_newton, const double* tol_time, const double* fac,
+                               const tchem_gb_tadv* tadv, const double* state, const double* number_conc,
+                               double* t_out, double* dt_out, double* state_out, int32_t* status,
+                               tchem_gb_sample_stats* stats, void* workspace, size_t workspace_bytes, void* stream);
+/* Aerosol RHS (src/core/impl/TChem_Impl_Aerosol_RHS.hpp:57-100) at each sample's state row:
+ * omega[nbatch][M] in ODE-vector order. */
+int tchem_gb_aero_rhs(const tchem_gb_mech* mech, const tchem_gb_aero* aero, int nbatch, const double* state,
+                      const double* number_conc, double* omega, void* stream);
+
+/* Solver settings file of the host-model driver interface (TChem::Driver::createNumerics,
+ * src/core/TChem_Driver.cpp:152-187): the solver_info mapping of a YAML file with the reference's
+ * keys and defaults (a key that is absent or does not convert takes its default): atol_newton
+ * 1e-10, rtol_newton 1e-6, dtmin 1e-8, atol_time 1e-12, rtol_time 1e-4, max_newton_iterations
+ * 100, max_num_time_iterations 1000, team_size -1, vector_size -1, verbose false. */
+typedef struct tchem_gb_numerics {
+  double atol_newton, rtol_newton, dtmin, atol_time, rtol_time;
+  int32_t max_newton_iterations, max_num_time_iterations, team_size, vector_size, verbose;
+} tchem_gb_numerics;
+int tchem_gb_numerics_read(const char* yaml_path, tchem_gb_numerics* out);
+
 /* Measurement helper (no counterpart in the reference): FMA throughput of the current device in
  * FLOP/s for FP64 (fp64 = 1) or FP32, from independent FMA chains on every SM. These are the
  * roofline denominators of the FP64-bound plain form and the FP32-bound mixed form. */

@@ -229,4 +229,25 @@ struct NetProductionRates {
   }
 };
 
+// Gas-aerosol (SIMPOL.1) time advance (TChem::AerosolChemistry, src/core/TChem_AerosolChemistry.hpp:51-103);
+// device arrays: tol_time[M][2], number_conc[nbatch][nParticles], state rows [rho, p, T, gas,
+// particles]; fac is not read.
+struct AerosolChemistry {
+  static size_t getWorkSpaceSize(const KineticModel& kmcd, const AerosolModel& amcd, int nbatch) {
+    const size_t n = tchem_gb_aero_workspace_bytes(kmcd.handle(), amcd.handle(), nbatch);
+    if (n == 0) check(TCHEM_GB_ERR_ARG, "tchem_gb_aero_workspace_bytes");
+    return n;
+  }
+  static void runDeviceBatch(void* stream, const double* tol_newton, const double* tol_time, const double* fac,
+                             const tchem_gb_tadv* tadv, const double* state, const double* number_conc,
+                             double* t_out, double* dt_out, double* state_out, const KineticModel& kmcd,
+                             const AerosolModel& amcd, int nbatch, int32_t* status, void* workspace = nullptr,
+                             size_t workspace_bytes = 0) {
+    check(tchem_gb_aero_time_advance(kmcd.handle(), amcd.handle(), nbatch, tol_newton, tol_time, fac, tadv, state,
+                                     number_conc, t_out, dt_out, state_out, status, nullptr, workspace,
+                                     workspace_bytes, stream),
+          "tchem_gb_aero_time_advance");
+  }
+};
+
 }  // namespace tchem_gb

@@ -5,37 +5,35 @@
 #include <string>
 #include <vector>
 
+#include "aero_host.hpp"
 #include "aerosol_model.hpp"
 #include "mech_host.hpp"
 
-struct tchem_gb_aero {
-  tchem_gb::AerosolModel am;
-  // Flattened copies backing tchem_gb_aero_view.
-  std::vector<int32_t> simpol_index;
-  std::vector<double> simpol_param;
-  tchem_gb_aero_view view{};
-
-  void build_view() {
-    simpol_index.clear();
-    simpol_param.clear();
-    for (const auto& s : am.simpol) {
-      const int32_t idx[3] = {s.aerosol_sp_index, s.gas_sp_index, s.compute_alpha ? 1 : 0};
-      simpol_index.insert(simpol_index.end(), idx, idx + 3);
-      const double par[7] = {s.B1, s.B2, s.B3, s.B4, s.diffusion_coeff, s.N_star, s.molecular_weight};
-      simpol_param.insert(simpol_param.end(), par, par + 7);
-    }
-    view.nSpec = am.nSpec;
-    view.nSpec_gas = am.nSpec_gas;
-    view.nConstSpec_gas = am.nConstSpec_gas;
-    view.nParticles = am.nParticles;
-    view.nSimpol = static_cast<int32_t>(am.simpol.size());
-    view.molecular_weights = am.molecular_weights.data();
-    view.aerosol_density = am.aerosol_density.data();
-    view.aerosol_kappa = am.aerosol_kappa.data();
-    view.simpol_index = simpol_index.data();
-    view.simpol_param = simpol_param.data();
+void tchem_gb_aero::build_view() {
+  simpol_index.clear();
+  simpol_param.clear();
+  for (const auto& s : am.simpol) {
+    const int32_t idx[3] = {s.aerosol_sp_index, s.gas_sp_index, s.compute_alpha ? 1 : 0};
+    simpol_index.insert(simpol_index.end(), idx, idx + 3);
+    const double par[7] = {s.B1, s.B2, s.B3, s.B4, s.diffusion_coeff, s.N_star, s.molecular_weight};
+    simpol_param.insert(simpol_param.end(), par, par + 7);
   }
-};
+  view.nSpec = am.nSpec;
+  view.nSpec_gas = am.nSpec_gas;
+  view.nConstSpec_gas = am.nConstSpec_gas;
+  view.nParticles = am.nParticles;
+  view.nSimpol = static_cast<int32_t>(am.simpol.size());
+  view.molecular_weights = am.molecular_weights.data();
+  view.aerosol_density = am.aerosol_density.data();
+  view.aerosol_kappa = am.aerosol_kappa.data();
+  view.simpol_index = simpol_index.data();
+  view.simpol_param = simpol_param.data();
+}
+
+tchem_gb_aero::~tchem_gb_aero() {
+  for (auto* t : device_tables)
+    if (t) tchem_gb::destroy_aero_device_tables(t);
+}
 
 using tchem_gb::set_last_error;
 

@@ -9,24 +9,12 @@
 #include <vector>
 
 #include "advance.hpp"
+#include "capi_internal.hpp"
 #include "kernels.hpp"
 #include "kernels_mixed.hpp"
 #include "mech_host.hpp"
 
 namespace tchem_gb {
-
-namespace {
-
-constexpr int kMaxGroups = 16;
-constexpr size_t kHeaderBytes = 256;  // queue[16] @0, error word @64, counts[16] @128
-constexpr int kMaxWarpsPerBlock = 8;
-
-size_t up256(size_t b) { return (b + 255) & ~size_t(255); }
-
-struct DeviceInfo {
-  int sm_count = 0;
-  int max_smem_optin = 0;
-};
 
 DeviceInfo device_info(int dev) {
   static std::mutex mu;
@@ -48,6 +36,58 @@ DeviceTables* tables_for(const tchem_gb_mech* mech, int dev) {
   if (!m->device_tables[dev]) m->device_tables[dev] = upload_tables(*m->host_tables, dev);
   return m->device_tables[dev];
 }
+
+// Library-owned workspace per device (used when the caller passes none).
+namespace {
+struct OwnedWorkspace {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+std::mutex g_ws_mu;
+std::vector<OwnedWorkspace> g_ws;
+}  // namespace
+
+void* owned_workspace(int dev, size_t bytes) {
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  if (static_cast<int>(g_ws.size()) <= dev) g_ws.resize(dev + 1);
+  OwnedWorkspace& w = g_ws[dev];
+  if (w.bytes < bytes) {
+    if (w.ptr) {
+      cudaDeviceSynchronize();
+      cudaFree(w.ptr);
+      w.ptr = nullptr;
+      w.bytes = 0;
+    }
+    const size_t want = std::max(bytes, size_t(1) << 20);
+    if (cudaMalloc(&w.ptr, want) != cudaSuccess) {
+      cudaGetLastError();
+      throw std::bad_alloc();
+    }
+    w.bytes = want;
+  }
+  return w.ptr;
+}
+
+void* owned_workspace_peek(int dev) {
+  std::lock_guard<std::mutex> lk(g_ws_mu);
+  return static_cast<int>(g_ws.size()) > dev ? g_ws[dev].ptr : nullptr;
+}
+
+int fail(int code, const std::string& msg) {
+  set_last_error(msg);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* where) {
+  return fail(TCHEM_GB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+namespace {
+
+constexpr int kMaxGroups = 16;
+constexpr int kMaxWarpsPerBlock = 8;
+
+size_t up256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct GroupPlan {
   std::vector<int> mechs;  // global mechanism indices in slot order
@@ -168,48 +208,7 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
   return plan;
 }
 
-// Library-owned workspace per device (used when the caller passes none).
-struct OwnedWorkspace {
-  void* ptr = nullptr;
-  size_t bytes = 0;
-};
-std::mutex g_ws_mu;
-std::vector<OwnedWorkspace> g_ws;
 
-void* owned_workspace(int dev, size_t bytes) {
-  std::lock_guard<std::mutex> lk(g_ws_mu);
-  if (static_cast<int>(g_ws.size()) <= dev) g_ws.resize(dev + 1);
-  OwnedWorkspace& w = g_ws[dev];
-  if (w.bytes < bytes) {
-    if (w.ptr) {
-      cudaDeviceSynchronize();
-      cudaFree(w.ptr);
-      w.ptr = nullptr;
-      w.bytes = 0;
-    }
-    const size_t want = std::max(bytes, size_t(1) << 20);
-    if (cudaMalloc(&w.ptr, want) != cudaSuccess) {
-      cudaGetLastError();
-      throw std::bad_alloc();
-    }
-    w.bytes = want;
-  }
-  return w.ptr;
-}
-
-void* owned_workspace_peek(int dev) {
-  std::lock_guard<std::mutex> lk(g_ws_mu);
-  return static_cast<int>(g_ws.size()) > dev ? g_ws[dev].ptr : nullptr;
-}
-
-int fail(int code, const std::string& msg) {
-  set_last_error(msg);
-  return code;
-}
-
-int cuda_fail(cudaError_t e, const char* where) {
-  return fail(TCHEM_GB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
-}
 
 tchem_gb_advance_opts opts_or_default(const tchem_gb_advance_opts* opts) {
   tchem_gb_advance_opts o{};

@@ -1,4 +1,5 @@
 // C ABI: mechanism and scenario entry points (host only).
+#include <cctype>
 #include <cstring>
 #include <fstream>
 #include <memory>
@@ -7,6 +8,7 @@
 #include <string>
 
 #include "mech_host.hpp"
+#include "yaml_lite.hpp"
 
 namespace tchem_gb {
 
@@ -266,6 +268,72 @@ int tchem_gb_scenario_external_forcing(const char* yaml_path, const tchem_gb_mec
     return TCHEM_GB_OK;
   } catch (const std::exception& e) {
     set_last_error(e.what());
+    return TCHEM_GB_ERR_PARSE;
+  }
+}
+
+namespace {
+
+// yaml-cpp's Node::as<T>(fallback): the fallback when the key is absent or does not convert.
+double num_or(const tchem_gb::yaml::Node* n, const char* key, double fallback) {
+  const tchem_gb::yaml::Node* v = n ? n->get(key) : nullptr;
+  if (!v || !v->is_scalar()) return fallback;
+  try {
+    size_t used = 0;
+    const double x = std::stod(v->scalar, &used);
+    return used == v->scalar.size() ? x : fallback;
+  } catch (...) {
+    return fallback;
+  }
+}
+
+int32_t int_or(const tchem_gb::yaml::Node* n, const char* key, int32_t fallback) {
+  const tchem_gb::yaml::Node* v = n ? n->get(key) : nullptr;
+  if (!v || !v->is_scalar()) return fallback;
+  try {
+    size_t used = 0;
+    const long x = std::stol(v->scalar, &used);
+    return used == v->scalar.size() ? static_cast<int32_t>(x) : fallback;
+  } catch (...) {
+    return fallback;
+  }
+}
+
+int32_t bool_or(const tchem_gb::yaml::Node* n, const char* key, int32_t fallback) {
+  const tchem_gb::yaml::Node* v = n ? n->get(key) : nullptr;
+  if (!v || !v->is_scalar()) return fallback;
+  std::string s = v->scalar;
+  for (auto& ch : s) ch = static_cast<char>(std::tolower(static_cast<unsigned char>(ch)));
+  if (s == "true" || s == "yes" || s == "y" || s == "on") return 1;
+  if (s == "false" || s == "no" || s == "n" || s == "off") return 0;
+  return fallback;
+}
+
+}  // namespace
+
+int tchem_gb_numerics_read(const char* yaml_path, tchem_gb_numerics* out) {
+  if (!yaml_path || !out) {
+    set_last_error("tchem_gb_numerics_read: null argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  try {
+    const tchem_gb::yaml::NodePtr root = tchem_gb::yaml::parse_file(yaml_path);
+    const tchem_gb::yaml::Node* si = root ? root->get("solver_info") : nullptr;
+    tchem_gb_numerics n{};
+    n.atol_newton = num_or(si, "atol_newton", 1e-10);
+    n.rtol_newton = num_or(si, "rtol_newton", 1e-6);
+    n.dtmin = num_or(si, "dtmin", 1e-8);
+    n.atol_time = num_or(si, "atol_time", 1e-12);
+    n.rtol_time = num_or(si, "rtol_time", 1e-4);
+    n.max_newton_iterations = int_or(si, "max_newton_iterations", 100);
+    n.max_num_time_iterations = int_or(si, "max_num_time_iterations", 1000);
+    n.team_size = int_or(si, "team_size", -1);
+    n.vector_size = int_or(si, "vector_size", -1);
+    n.verbose = bool_or(si, "verbose", 0);
+    *out = n;
+    return TCHEM_GB_OK;
+  } catch (const std::exception& e) {
+    set_last_error(std::string("tchem_gb_numerics_read: ") + e.what());
     return TCHEM_GB_ERR_PARSE;
   }
 }

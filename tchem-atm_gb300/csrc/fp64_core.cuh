@@ -31,6 +31,12 @@ struct Ctx {
   tchem_gb_sample_stats st;
 };
 
+// Size of the Newton system of a context (the aerosol context of kernels_aero.cu has its own).
+template <int NPL>
+__device__ __forceinline__ int sys_dim(const Ctx<NPL>& c) {
+  return c.L.m;
+}
+
 template <int NPL>
 __device__ __forceinline__ void publish(Ctx<NPL>& c, const double (&y)[NPL]) {
 #pragma unroll
@@ -97,10 +103,11 @@ __device__ __forceinline__ void newton_matrix(Ctx<NPL>& c, const double (&y)[NPL
 }
 
 // In-place LU with partial pivoting (first maximum in current row order), row swaps.
-template <int NPL>
-__device__ __forceinline__ bool lu_factor(Ctx<NPL>& c) {
+// C: a per-sample context (Ctx, or the aerosol context) with W.A, W.piv, lda, lane and st.
+template <class C>
+__device__ __forceinline__ bool lu_factor(C& c) {
   double* A = c.W.A;
-  const int m = c.L.m, lda = c.lda, lane = c.lane;
+  const int m = sys_dim(c), lda = c.lda, lane = c.lane;
   for (int k = 0; k < m; ++k) {
     double best = -1.0;
     int bi = m;
@@ -145,11 +152,11 @@ __device__ __forceinline__ bool lu_factor(Ctx<NPL>& c) {
 }
 
 // x = A^{-1} b with the factors of lu_factor.
-template <int NPL>
-__device__ __forceinline__ void lu_solve(Ctx<NPL>& c, const double (&b)[NPL], double (&x)[NPL]) {
+template <int NPL, class C>
+__device__ __forceinline__ void lu_solve(C& c, const double (&b)[NPL], double (&x)[NPL]) {
   const double* A = c.W.A;
   double* w = c.W.w;
-  const int m = c.L.m, lda = c.lda, lane = c.lane;
+  const int m = sys_dim(c), lda = c.lda, lane = c.lane;
 #pragma unroll
   for (int k = 0; k < NPL; ++k) {
     const int i = lane + 32 * k;
@@ -189,9 +196,9 @@ struct NewtonSettings {
   double atol, rtol;
 };
 
-// Solves y - coef f(y) = rhs from the guess in y.
-template <int NPL>
-__device__ __forceinline__ bool newton(Ctx<NPL>& c, double (&y)[NPL], const double (&rhs_v)[NPL], double coef, const NewtonSettings& s) {
+// Solves y - coef f(y) = rhs from the guess in y. rhs and newton_matrix resolve on the context type.
+template <int NPL, class C>
+__device__ __forceinline__ bool newton(C& c, double (&y)[NPL], const double (&rhs_v)[NPL], double coef, const NewtonSettings& s) {
   for (int it = 0; it < s.max_newton; ++it) {
     double f[NPL], g[NPL], dx[NPL];
     rhs(c, y, f);
@@ -206,7 +213,7 @@ __device__ __forceinline__ bool newton(Ctx<NPL>& c, double (&y)[NPL], const doub
     double sdx = 0.0, sy = 0.0;
 #pragma unroll
     for (int k = 0; k < NPL; ++k) {
-      if (c.lane + 32 * k < c.L.m) {
+      if (c.lane + 32 * k < sys_dim(c)) {
         y[k] += dx[k];
         sdx += dx[k] * dx[k];
         sy += y[k] * y[k];
@@ -228,8 +235,8 @@ struct Tape {
 };
 
 // TR-BDF2 integration of one sample (same algorithm as the oracle's Sample::integrate).
-template <int NPL>
-__device__ int integrate(Ctx<NPL>& c, double (&y)[NPL], const double (&atol)[NPL], const double (&rtol)[NPL],
+template <int NPL, class C>
+__device__ int integrate(C& c, double (&y)[NPL], const double (&atol)[NPL], const double (&rtol)[NPL],
                          double t_beg, double t_end, double dt_in, double dt_min, double dt_max, int max_iters,
                          const NewtonSettings& s, double& t_out, double& dt_out, const Tape& tape = Tape{}) {
   if (dt_in < 0.0) return TCHEM_GB_SAMPLE_NEGATIVE_DT;
@@ -239,7 +246,7 @@ __device__ int integrate(Ctx<NPL>& c, double (&y)[NPL], const double (&atol)[NPL
   const double cn = (1.0 - gamma) * (1.0 - gamma) / (gamma * (2.0 - gamma));
   const double kappa = (-3.0 * gamma * gamma + 4.0 * gamma - 2.0) / (12.0 * (2.0 - gamma));
   const double e0 = 1.0 / gamma, e1 = -1.0 / (gamma * (1.0 - gamma)), e2 = 1.0 / (1.0 - gamma);
-  const int m = c.L.m;
+  const int m = sys_dim(c);
 
   double fn[NPL], fg[NPL], f1[NPL], yg[NPL], y1[NPL], rv[NPL];
   double t = t_beg, dt = dt_in;

@@ -75,6 +75,50 @@ struct E3smParams {
 };
 cudaError_t launch_e3sm(const E3smParams& P, E3smOut kind, int sm_count, cudaStream_t stream);
 
+// Gas-aerosol problem (SIMPOL.1 phase transfer) of the plain form (kernels_aero.cu): one warp per
+// sample, one gas mechanism and one aerosol model per call. The ODE vector is [active gas species,
+// particle 0's aerosol species, particle 1's, ...], M = m_gas + nP * nA entries.
+struct AeroDev {
+  int32_t nA, nP, nS, m_gas, M;  // aerosol species per particle, particles, SIMPOL entries, active gas, ODEs
+  const int32_t* sim_idx;        // [nS][3]: aerosol ODE index (particle 0), gas index, alpha from N*
+  const double* sim_par;         // [nS][7]: B1..B4, diffusion coefficient, N*, gas molecular weight
+  const double* density;         // [nA] kg/m3
+  const double* mw;              // [nA] kg/mol
+  double vol0, mass0, moles0;    // particle volume, mass and moles floors
+};
+// Byte offsets of one warp's shared-memory sections (computed on the host, read by the kernel).
+struct AeroWarpLayout {
+  uint32_t x, f, keff, q, w, piv, simc, part, dsim, nc, A, bytes;
+};
+AeroWarpLayout aero_warp_layout(const MechLayout& L, const AeroDev& A, int lda, bool matrix_in_smem);
+struct AeroParams {
+  MechDev mech;                   // gas tables (plain form)
+  AeroDev aero;
+  AeroWarpLayout wl;
+  int32_t B, n_gas, state_dim;    // samples, gas species (active + constant), state row width
+  const double* number_conc;      // [B][nP]
+  const double* tol_newton;       // [2]
+  const double* tol_time;         // [M][2]
+  const tchem_gb_tadv* tadv;      // [B]
+  const double* state;            // [B][state_dim]: rho, p, T, gas species, particles
+  double* state_out;              // [B][state_dim] (may alias state)
+  double* t_out;                  // [B] in/out
+  double* dt_out;                 // [B]
+  int32_t* status;                // [B]
+  tchem_gb_sample_stats* stats;   // [B] or null
+  double* omega;                  // right-hand-side mode: [B][M]
+  double* gmat;                   // per-warp matrix slots in global memory (when not in smem)
+  int64_t gmat_stride;
+  int32_t lda;
+  int32_t matrix_in_smem;
+  int32_t* queue;
+  int32_t* error_word;
+};
+constexpr int kAeroMaxOde = 320;  // largest ODE system of the aerosol kernel (10 entries per lane)
+const void* aero_kernel_ptr(int M, bool rhs_only);
+cudaError_t launch_aero(const AeroParams& P, bool rhs_only, int grid, int warps_per_block, size_t smem,
+                        cudaStream_t stream);
+
 // Groups samples by mechanism group: items[g * B + k], counts[g] (kernels_fp64.cu).
 struct GroupMap {
   int32_t group_of_mech[kMaxMechs];

@@ -5,7 +5,8 @@ set_scenario_photolysis_rates, set_scenario_external_forcing).
 Compute: hand-written sm_103a CUDA kernels behind the C ABI in include/tchem_gb.h
 (AtmosphericChemistry.runDeviceBatch / runHostBatch, kforward, reaction_rates, jacobian; the E3SM
 gas chemistry in tchem_gb.e3sm: AtmosphericChemistryE3SM, ReactionRates, RateofProgress,
-NetProductionRates).
+NetProductionRates; the gas-aerosol (SIMPOL.1) chemistry in tchem_gb.aerosol: AerosolModel,
+AerosolChemistry, AerosolRHS).
 """
 from .mechanism import (KineticModel, scenario_batch_size, set_scenario_conditions,  # noqa: F401
                         set_scenario_external_forcing, set_scenario_photolysis_rates)

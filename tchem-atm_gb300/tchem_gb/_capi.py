@@ -60,6 +60,14 @@ class AeroView(C.Structure):
     ]
 
 
+class Numerics(C.Structure):
+    """tchem_gb_numerics: the solver settings of the host-model driver interface."""
+    _fields_ = [("atol_newton", C.c_double), ("rtol_newton", C.c_double), ("dtmin", C.c_double),
+                ("atol_time", C.c_double), ("rtol_time", C.c_double), ("max_newton_iterations", C.c_int32),
+                ("max_num_time_iterations", C.c_int32), ("team_size", C.c_int32), ("vector_size", C.c_int32),
+                ("verbose", C.c_int32)]
+
+
 class AdvanceOpts(C.Structure):
     _fields_ = [("form", C.c_int32), ("threads_per_sample", C.c_int32), ("reserved", C.c_int32 * 6)]
 
@@ -133,6 +141,11 @@ def lib() -> C.CDLL:
         "tchem_gb_e3sm_workspace_bytes": (C.c_size_t, [vp, C.c_int, popts]),
         "tchem_gb_e3sm_time_advance": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp,
                                                  vp, vp, C.c_size_t, popts, vp]),
+        "tchem_gb_aero_workspace_bytes": (C.c_size_t, [vp, vp, C.c_int]),
+        "tchem_gb_aero_time_advance": (C.c_int, [vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                                 vp, C.c_size_t, vp]),
+        "tchem_gb_aero_rhs": (C.c_int, [vp, vp, C.c_int, vp, vp, vp, vp]),
+        "tchem_gb_numerics_read": (C.c_int, [C.c_char_p, C.POINTER(Numerics)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

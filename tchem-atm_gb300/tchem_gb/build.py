@@ -1,4 +1,6 @@
-"""Builds libtchem_gb.so (the engine: sm_103a CUDA kernels + C ABI) in-tree.
+"""Builds libtchem_gb.so (the engine: sm_103a CUDA kernels + C ABI) in-tree, and beside it
+libtchem_gb_driver.so (the host-model driver interface of include/tchem_gb_driver.h, host code
+over libtchem_gb.so).
 
 Translation units are compiled in parallel with nvcc and linked into
 ``tchem-atm_gb300/tchem_gb/libtchem_gb.so``. Nothing here depends on torch.
@@ -16,6 +18,8 @@ PKG_DIR = Path(__file__).resolve().parent
 SRC_DIR = PKG_DIR.parent / "csrc"
 BUILD_DIR = PKG_DIR.parent / "_build"
 LIB_PATH = PKG_DIR / "libtchem_gb.so"
+DRIVER_LIB_PATH = PKG_DIR / "libtchem_gb_driver.so"
+DRIVER_DIR = SRC_DIR / "driver"
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
@@ -49,17 +53,24 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None, force: bo
     BUILD_DIR.mkdir(exist_ok=True)
     srcs = sources()
     extra = list(extra_flags or [])
-    if not force and LIB_PATH.exists():
-        newest = max(p.stat().st_mtime for p in srcs + list(SRC_DIR.glob("*.h*")) + list(SRC_DIR.glob("*.cuh")))
-        hdr = PKG_DIR.parent.parent / "include" / "tchem_gb.h"
-        if hdr.exists():
-            newest = max(newest, hdr.stat().st_mtime)
-        if LIB_PATH.stat().st_mtime > newest and not extra:
+    driver_srcs = sorted(DRIVER_DIR.glob("*.cpp"))
+    if not force and LIB_PATH.exists() and DRIVER_LIB_PATH.exists():
+        deps = srcs + driver_srcs + list(SRC_DIR.glob("*.h*")) + list(SRC_DIR.glob("*.cuh"))
+        deps += [h for h in (PKG_DIR.parent.parent / "include").glob("tchem_gb*.h")]
+        newest = max(p.stat().st_mtime for p in deps)
+        if min(LIB_PATH.stat().st_mtime, DRIVER_LIB_PATH.stat().st_mtime) > newest and not extra:
             return LIB_PATH
     workers = min(len(srcs), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
         objs = list(ex.map(lambda s: _compile(nvcc, s, extra), srcs))
     cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(LIB_PATH), *map(str, objs), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    # the driver interface: host code linked against the engine, found beside it at run time
+    dobjs = [_compile(nvcc, s, extra) for s in driver_srcs]
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(DRIVER_LIB_PATH), *map(str, dobjs), "-L", str(PKG_DIR),
+           "-ltchem_gb", "-lcudart", "-Xlinker", "-rpath=$ORIGIN"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -18,7 +18,10 @@ Everything copied is data the reference's own tests and examples use:
   * the aerosol (SIMPOL.1 phase transfer) inputs and goldens: the Simpol and CB05CL_AE5_w_simpolSOA
     example files, the SIMPOL RHS golden (src/unit-tests/references/partmc_integration/simpol/),
     the TR-BDF2 goldens src/unit-tests/TinesODE/references/*.hdf5 (decoded at their raw data
-    offset) and the CAMP SIMPOL trajectory.
+    offset) and the CAMP SIMPOL trajectory,
+  * the host-model driver interface test (src/unit-tests/TChem_Driver/): its solver settings file
+    and its three reference outputs (gas species names, aerosol species properties, the state
+    after one 30 s step).
 Run settings of each case come from the reference's scripts and are recorded in manifest.json.
 """
 from __future__ import annotations
@@ -115,6 +118,17 @@ def main(ref: Path) -> None:
     np.save(aero_dir / "camp_simpol.npy",
             np.loadtxt(ref / RUNS / "Simpol" / "camp_out" / "SIMPOL_phase_transfer_results.txt"))
 
+    driver_dir = HERE / "driver"
+    driver_dir.mkdir(exist_ok=True)
+    driver_copies = {
+        "config_solver.yaml": "src/unit-tests/TChem_Driver/config_solver.yaml",
+        "gas_species_names_ref.txt": "src/unit-tests/TChem_Driver/references/gas_species_names_ref.txt",
+        "aero_species_props_ref.txt": "src/unit-tests/TChem_Driver/references/aero_species_props_ref.txt",
+        "output_ref.txt": "src/unit-tests/TChem_Driver/references/output_ref.txt",
+    }
+    for dst, src in driver_copies.items():
+        shutil.copyfile(ref / src, driver_dir / dst)
+
     manifest = {
         "cb05cl_ae5_full_gas": {
             "source": "src/unit-tests/CB05CL_AE5/references/full_gas.hdf5",
@@ -163,6 +177,19 @@ def main(ref: Path) -> None:
             "camp_simpol.npy": {"source": f"{RUNS}/Simpol/camp_out/SIMPOL_phase_transfer_results.txt",
                                 "columns": "time [s], then ethanol, ethanol_aq, H2O_aq as pairs of CAMP columns"},
         },
+        "driver": {
+            "files": {f"driver/{dst}": src for dst, src in driver_copies.items()},
+            "run": "src/unit-tests/TChem_Driver/TChem_Driver.c, CMakeLists.txt (DriverInterface)",
+            "gas": "aerosol/cb05_soa_config_full_gas.yaml", "aero": "aerosol/cb05_soa_mechanism_aero.yaml",
+            "solver": "driver/config_solver.yaml", "batch": 1,
+            "state": {"1": 81060.0, "2": 270.5, "36": 0.001, "50": 0.06, "51": 1e-06, "81": 1e8},
+            "particles": {"first_species": 1e-08, "number_conc": 1e4},
+            "del_t": 30.0,
+            "outputs": {"gas_species_names_ref.txt": "one name per line",
+                        "aero_species_props_ref.txt": "name density mw kappa, printf %s %f %f %f",
+                        "output_ref.txt": "the state row after TChem_doTimestep, printf %e"},
+            "criterion": "names and properties: identical lines; state: numpy isclose (rtol 1e-5, atol 1e-8) "
+                         "(src/unit-tests/TChem_Driver/compare_files.py)"},
         "e3sm": {
             "files": {f"e3sm/{dst}": src for dst, src in e3sm_copies.items()},
             "reaction-rates.dat": {"run": "src/unit-tests/TChem_Test_ReactionRates.hpp:28-50",

@@ -8,6 +8,7 @@ from tchem_gb import KineticModel, _capi
 from tchem_gb.generator import MechanismSpec, mechanism_yaml
 
 ERR_ARG = 1
+ERR_UNSUPPORTED = 4
 
 
 def _km():
@@ -78,3 +79,41 @@ def test_e3sm_entry_points_reject_bad_arguments():
     assert f(km.handle, 0, *([nul] * 6), 0, nul, nul, nul, nul, nul, nul, nul, 0, C.byref(o), nul) == 0
     o.form = 9
     assert f(km.handle, 4, *([buf] * 6), 0, nul, *([buf] * 4), nul, nul, 0, C.byref(o), nul) == ERR_ARG
+
+
+def test_aerosol_entry_points_reject_bad_arguments():
+    """tchem_gb_aero_time_advance / _rhs / _workspace_bytes: host-side checks of the model pair
+    (mechanism tables built on the host, including a mechanism without reactions) before any
+    device work."""
+    from helpers import GOLDEN
+    from tchem_gb.aerosol import AerosolModel
+    A = GOLDEN / "aerosol"
+    L = _capi.lib()
+    nul = C.c_void_p(0)
+    gas = KineticModel.from_file(A / "simpol_config_gas.yaml")  # no gas reactions
+    am = AerosolModel.from_file(A / "simpol_phase_transfer.yaml", gas)
+    adv = L.tchem_gb_aero_time_advance
+    assert adv(gas.handle, am.handle, 0, *([nul] * 12), 0, nul) == 0  # empty batch
+    assert adv(gas.handle, am.handle, 4, *([nul] * 12), 0, nul) == ERR_ARG
+    assert b"null" in L.tchem_gb_last_error()
+    assert adv(nul, am.handle, 4, *([nul] * 12), 0, nul) == ERR_ARG
+    assert L.tchem_gb_aero_rhs(gas.handle, am.handle, 0, nul, nul, nul, nul) == 0
+    assert L.tchem_gb_aero_rhs(gas.handle, am.handle, 2, nul, nul, nul, nul) == ERR_ARG
+    cb = KineticModel.from_file(A / "cb05_soa_config_full_gas.yaml")
+    cb_am = AerosolModel.from_file(A / "cb05_soa_mechanism_aero.yaml", cb)
+    assert adv(cb.handle, cb_am.handle, 0, *([nul] * 12), 0, nul) == 0
+    assert adv(cb.handle, am.handle, 0, *([nul] * 12), 0, nul) == ERR_ARG  # model built on another gas mechanism
+    assert b"another gas mechanism" in L.tchem_gb_last_error()
+    assert L.tchem_gb_aero_workspace_bytes(cb.handle, am.handle, 4) == 0
+    am.set_number_of_particles(200)  # 1 + 2 * 200 ODEs
+    assert adv(gas.handle, am.handle, 4, *([nul] * 12), 0, nul) == ERR_UNSUPPORTED
+    assert b"at most 320" in L.tchem_gb_last_error()
+    # a SIMPOL gas species held constant: the transfer would change a constant species
+    const_gas = KineticModel.from_string((A / "simpol_config_gas.yaml").read_text().replace(
+        "constant_species:\n- description: tracer-CONSTANT\n  name: M\nspecies:\n- description: ETHANOL\n  name: ethanol",
+        "constant_species:\n- description: tracer-CONSTANT\n  name: M\n- description: ETHANOL\n  name: ethanol\n"
+        "species:\n- description: tracer\n  name: X"))
+    assert const_gas.nConstSpec == 2
+    const_am = AerosolModel.from_file(A / "simpol_phase_transfer.yaml", const_gas)
+    assert adv(const_gas.handle, const_am.handle, 0, *([nul] * 12), 0, nul) == ERR_UNSUPPORTED
+    assert b"not an active species" in L.tchem_gb_last_error()
