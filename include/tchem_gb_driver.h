@@ -1,6 +1,6 @@
 /* Host-model driver interface: the extern "C" functions a host model (PartMC) binds to drive the
  * gas-aerosol chemistry one time step at a time, with the reference's names, argument order and
- * conventions (src/core/TChem_Driver.hpp:106-132, src/core/TChem_Driver.cpp:87-640), exported by
+ * conventions (src/core/TChem_Driver.hpp:106-132, src/core/TChem_Driver.cpp:88-640), exported by
  * libtchem_gb_driver.so (which links libtchem_gb.so).
  *
  * One driver per process. initialize() reads the gas mechanism, the aerosol model and the solver

@@ -1,5 +1,5 @@
 // Host-model driver interface (libtchem_gb_driver.so): the reference's TChem::Driver and its
-// extern "C" functions (src/core/TChem_Driver.hpp:28-132, src/core/TChem_Driver.cpp:87-640) over
+// extern "C" functions (src/core/TChem_Driver.hpp:28-132, src/core/TChem_Driver.cpp:88-640) over
 // the engine's C ABI. The state and number-concentration rows live on the host, as the
 // reference's do; TChem_doTimestep copies them to the device, runs the gas-aerosol TR-BDF2 kernel
 // (tchem_gb_aero_time_advance) and copies them back. Device buffers are allocated on the first
