@@ -86,6 +86,9 @@ def parse() -> argparse.Namespace:
                     help="samples of the discrete-adjoint leg (1800 s horizon, FP64); 0 skips it")
     ap.add_argument("--e3sm-samples", type=int, default=65536,
                     help="samples of the E3SM leg (the reference's 80-column uci scenario tiled); 0 skips it")
+    ap.add_argument("--aerosol-samples", type=int, default=0,
+                    help="samples of the gas-aerosol (SIMPOL.1) leg: the reference driver test's CB05CL_AE5 + SOA "
+                         "sample perturbed, one 30 s driver time step (83 ODEs, plain FP64); 0 skips it")
     return ap.parse_args()
 
 
@@ -441,6 +444,98 @@ def e3sm_leg(B: int, cpu_seconds: float, dev, stream) -> dict:
                                        f"samples on {cores} threads ({el:.2f} s)"}}
 
 
+# ---- gas-aerosol chemistry (SIMPOL.1) ---------------------------------------------------------
+
+AERO_DIR = ROOT / "tests" / "golden" / "aerosol"
+DRIVER_DIR = ROOT / "tests" / "golden" / "driver"
+
+
+def aerosol_leg(B: int, cpu_seconds: float, dev, stream) -> dict:
+    """The gas-aerosol TR-BDF2 advance (AerosolChemistry::runDeviceBatch, plain FP64) on the
+    reference driver test's case: CB05CL_AE5 with four SIMPOL SOA transfers and one particle
+    (83 ODEs), its state and number concentration perturbed per sample (seeded, x0.5..1.5), one
+    30 s time step with its solver settings (tolerances 1e-12 / 1e-6, Newton 1e-6 / 1e-4, first
+    step 1e-12); the first 16 end states against the oracle, sample 0 unperturbed against the
+    driver test's output, and the oracle on the host cores."""
+    import torch
+    from oracle import AerosolOracle
+    from tchem_gb import tadv_to_device, time_advance_array
+    from tchem_gb.aerosol import AerosolChemistry, AerosolModel
+    man = json.loads((ROOT / "tests" / "golden" / "manifest.json").read_text())["driver"]
+    km = KineticModel.from_file(AERO_DIR / "cb05_soa_config_full_gas.yaml")
+    am = AerosolModel.from_file(AERO_DIR / "cb05_soa_mechanism_aero.yaml", km)
+    n = _capi.Numerics()
+    _capi.check(_capi.lib().tchem_gb_numerics_read(str(DRIVER_DIR / "config_solver.yaml").encode(), C.byref(n)),
+                "tchem_gb_numerics_read")
+    st0 = np.zeros(am.state_dim)
+    for k, v in man["state"].items():
+        st0[int(k)] = v
+    st0[3 + km.nSpec] = man["particles"]["first_species"]
+    rng = np.random.default_rng(11)
+    state = np.tile(st0, (B, 1))
+    state[1:, 3:] *= rng.uniform(0.5, 1.5, (B - 1, am.state_dim - 3))
+    nc = np.full((B, am.nParticles), man["particles"]["number_conc"])
+    nc[1:] *= rng.uniform(0.5, 1.5, (B - 1, 1))
+    del_t = man["del_t"]
+    tadv = time_advance_array(B, tend=del_t, dt=n.dtmin, dtmin=n.dtmin, dtmax=del_t,
+                              max_num_newton_iterations=n.max_newton_iterations,
+                              num_time_iterations_per_interval=n.max_num_time_iterations)
+    tol_newton = [n.atol_newton, n.rtol_newton]
+    tol_time = np.tile([n.atol_time, n.rtol_time], (am.n_ode, 1))
+    d = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64)).to(dev)  # noqa: E731
+    d_state, d_nc, d_tadv = d(state), d(nc), tadv_to_device(tadv, dev)
+    d_tn, d_tt = d(tol_newton), d(tol_time)
+    out = torch.empty_like(d_state)
+    t = torch.zeros(B, dtype=torch.float64, device=dev)
+    dt = torch.zeros_like(t)
+    stats = torch.zeros(B * 8, dtype=torch.int32, device=dev)
+    ws = torch.empty(AerosolChemistry.getWorkSpaceSize(km, am, B), dtype=torch.uint8, device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+
+    def run():
+        t.zero_()
+        return AerosolChemistry.runDeviceBatch(d_tn, d_tt, None, d_tadv, d_state, d_nc, t, dt, out, km, am,
+                                               stats=stats, workspace=ws, stream=stream)
+    run()
+    torch.cuda.synchronize(dev)
+    best = float("inf")
+    for _ in range(3):
+        ev[0].record(stream)
+        status = run()
+        ev[1].record(stream)
+        torch.cuda.synchronize(dev)
+        best = min(best, ev[0].elapsed_time(ev[1]))
+    res = out.cpu().numpy()
+    st = np.frombuffer(stats.cpu().numpy().tobytes(), dtype=_capi.SAMPLE_STATS_DTYPE)
+    K = min(16, B)
+    ref, *_ = AerosolOracle(km, am).time_advance(tadv[:K], state[:K], nc[:K], tol_newton, tol_time)
+    golden = np.loadtxt(DRIVER_DIR / "output_ref.txt")
+    o = AerosolOracle(km, am, native=True)
+    m = K
+    t0 = time.perf_counter()
+    o.time_advance(tadv[:m], state[:m], nc[:m], tol_newton, tol_time)
+    el = time.perf_counter() - t0
+    m = int(min(B, max(K, K * round(cpu_seconds / max(el, 1e-6)))))
+    t0 = time.perf_counter()
+    o.time_advance(tadv[:m], state[:m], nc[:m], tol_newton, tol_time)
+    el = time.perf_counter() - t0
+    cores = os.cpu_count() or 1
+    diff = res[:K, 3:] - ref[:, 3:]
+    den = np.linalg.norm(ref[:, 3:], axis=0)
+    col = np.where(den > 1e-23, np.linalg.norm(diff, axis=0) / np.where(den > 1e-23, den, 1.0), 0.0)
+    return {"metric": "box-samples/s (gas-aerosol TR-BDF2, one 30 s driver step)", "value": B / (best * 1e-3),
+            "unit": "samples/s", "samples": B, "ms": best, "form": "plain", "dtype": "f64",
+            "workload": "reference driver test: CB05CL_AE5 + 4 SIMPOL SOA transfers, 1 particle, 83 ODEs, "
+                        "state and number concentration perturbed x0.5..1.5 per sample (seed 11), 30 s",
+            "status_ok": int((status.cpu().numpy() == 0).sum()),
+            "steps_mean": float(st["n_steps"].mean()), "rhs_mean": float(st["n_rhs"].mean()),
+            "accuracy": {"vs_oracle_norm_relative_max": float(col.max()), "oracle_samples": K,
+                         "sample0_vs_driver_test_output_isclose": bool(np.all(np.isclose(res[0], golden)))},
+            "cpu_baseline": {"value": m / el, "unit": "samples/s", "cores": cores, "kind": "port",
+                             "sample": f"first {m} samples, aerosol CPU restatement built for the host CPU, OpenMP "
+                                       f"over samples on {cores} threads ({el:.2f} s)"}}
+
+
 # ---- discrete adjoint -------------------------------------------------------------------------
 
 def adjoint_leg(km, state, tol_time, n: int, dev, stream) -> dict:
@@ -647,6 +742,9 @@ def engine_arm(args, world: int, rank: int, local: int):
 
     if rank == 0 and args.e3sm_samples > 0:
         line["e3sm"] = e3sm_leg(args.e3sm_samples, min(args.cpu_seconds, 5.0), dev, stream)
+
+    if rank == 0 and args.aerosol_samples > 0:
+        line["aerosol"] = aerosol_leg(args.aerosol_samples, min(args.cpu_seconds, 5.0), dev, stream)
 
     if not args.no_e2e:
         # end to end through the host-buffer C ABI: pinned host arrays in, results out, every copy
