@@ -35,6 +35,16 @@
  *                               ::runDeviceBatch, src/core/TChem_ReactionRates.hpp:59-72,
  *                               src/core/TChem_RateofProgress.hpp:60-75,
  *                               src/core/TChem_NetProductionRates.hpp:61-78
+ *   tchem_gb_aero_create_*, tchem_gb_aero_scenario_particles
+ *                               TChem::AerosolModelData (+ scenarioConditionParticles)
+ *                               src/core/TChem_AerosolModelData.cpp:60-300
+ *   tchem_gb_aero_time_advance  TChem::AerosolChemistry::runDeviceBatch
+ *                               src/core/TChem_AerosolChemistry.hpp:87-103
+ *   tchem_gb_aero_rhs           TChem::Impl::Aerosol_RHS::team_invoke
+ *                               src/core/impl/TChem_Impl_Aerosol_RHS.hpp:57-100
+ *   tchem_gb_numerics_read      TChem::Driver::createNumerics src/core/TChem_Driver.cpp:152-187
+ * The host-model driver functions themselves (initialize, TChem_doTimestep, ...) are in
+ * tchem_gb_driver.h (libtchem_gb_driver.so).
  */
 #ifndef TCHEM_GB_H
 #define TCHEM_GB_H
@@ -411,6 +421,14 @@ typedef struct tchem_gb_numerics {
   int32_t max_newton_iterations, max_num_time_iterations, team_size, vector_size, verbose;
 } tchem_gb_numerics;
 int tchem_gb_numerics_read(const char* yaml_path, tchem_gb_numerics* out);
+
+/* Tensor-core building block of the 300-species factorization (no counterpart in the reference):
+ * for each of ntiles tiles, D[128][N] -= A[128][32] * B[32][N] with TF32 operands and FP32
+ * accumulation on the 5th-generation tensor cores (tcgen05.mma kind::tf32, accumulator in TMEM),
+ * the trailing update of a blocked LU with 32-column panels. Row-major FP32 device arrays, tile t
+ * at A + t*128*32, B + t*32*N, D + t*128*N; N a multiple of 16 in [16, 256]. Bounded waits report
+ * through tchem_gb_device_error. Validation on a GPU is pending. */
+int tchem_gb_tc_tile_update_tf32(int ntiles, int N, const float* A, const float* B, float* D, void* stream);
 
 /* Measurement helper (no counterpart in the reference): FMA throughput of the current device in
  * FLOP/s for FP64 (fp64 = 1) or FP32, from independent FMA chains on every SM. These are the

@@ -117,3 +117,13 @@ def test_aerosol_entry_points_reject_bad_arguments():
     const_am = AerosolModel.from_file(A / "simpol_phase_transfer.yaml", const_gas)
     assert adv(const_gas.handle, const_am.handle, 0, *([nul] * 12), 0, nul) == ERR_UNSUPPORTED
     assert b"not an active species" in L.tchem_gb_last_error()
+
+
+def test_tensor_core_tile_update_checks_its_shape():
+    L = _capi.lib()
+    nul = C.c_void_p(0)
+    assert L.tchem_gb_tc_tile_update_tf32(0, 64, nul, nul, nul, nul) == 0  # no tiles
+    for n in (0, 8, 24, 272):
+        assert L.tchem_gb_tc_tile_update_tf32(1, n, nul, nul, nul, nul) == ERR_ARG
+    assert L.tchem_gb_tc_tile_update_tf32(2, 64, nul, nul, nul, nul) == ERR_ARG
+    assert b"null" in L.tchem_gb_last_error()
