@@ -301,8 +301,6 @@ int tchem_gb_aero_rhs(const tchem_gb_mech* mech, const tchem_gb_aero* aero, int 
   } catch (const std::exception& e) {
     return fail(TCHEM_GB_ERR_ARG, std::string(who) + ": " + e.what());
   }
-  cudaError_t e = cudaMemsetAsync(ws, 0, 64, stream);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync(workspace)");
   AeroParams P{};
   P.mech = t->dev;
   P.aero = A;
@@ -314,9 +312,9 @@ int tchem_gb_aero_rhs(const tchem_gb_mech* mech, const tchem_gb_aero* aero, int 
   P.state = state;
   P.omega = omega;
   P.lda = plan.lda;
-  P.queue = reinterpret_cast<int32_t*>(ws);
+  P.queue = nullptr;  // the RHS kernel strides over the samples
   P.error_word = reinterpret_cast<int32_t*>(ws + 64);
-  e = launch_aero(P, true, plan.grid, plan.warps, plan.smem, stream);
+  cudaError_t e = launch_aero(P, true, plan.grid, plan.warps, plan.smem, stream);
   if (e != cudaSuccess) return cuda_fail(e, "aerosol RHS kernel launch");
   return TCHEM_GB_OK;
 }

@@ -293,10 +293,17 @@ __global__ void __launch_bounds__(256, 1) aero_kernel(const __grid_constant__ Ae
   E.R = L.R;
 
   const int mg = P.aero.m_gas, M = P.aero.M, n = P.n_gas;
+  // the time advance pulls samples from the work queue; the RHS (uniform work) strides over them
+  int next = blockIdx.x * (blockDim.x >> 5) + warp;
   while (true) {
     int s = 0;
-    if (lane == 0) s = atomicAdd(P.queue, 1);
-    s = __shfl_sync(kFullMask, s, 0);
+    if constexpr (RHS_ONLY) {
+      s = next;
+      next += gridDim.x * (blockDim.x >> 5);
+    } else {
+      if (lane == 0) s = atomicAdd(P.queue, 1);
+      s = __shfl_sync(kFullMask, s, 0);
+    }
     if (s >= P.B) break;
     tchem_gb_tadv ta{};
     if constexpr (!RHS_ONLY) {
