@@ -196,6 +196,9 @@ def test_cpp_shim_compiles_links_and_parses(tmp_path):
         "  if (argc > 3) {  // an aerosol model over this gas mechanism\n"
         "    tchem_gb::AerosolModel am(argv[3], km);\n"
         '    std::printf("aero %d %d\\n", am.view().nSpec, am.view().nSimpol);\n'
+        "    if (argc > 4)  // referenced, not run: the gas-aerosol time advance of the C++ face links\n"
+        "      tchem_gb::AerosolChemistry::runDeviceBatch(nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,\n"
+        "                                                 nullptr, nullptr, nullptr, km, am, 0, nullptr);\n"
         "  }\n"
         "  tchem_gb_e3sm_view e = km.e3sm_view();\n"
         '  std::printf("%d %d\\n", e.nJPL, e.nAdjust);\n'
