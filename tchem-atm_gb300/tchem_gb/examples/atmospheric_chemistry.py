@@ -98,8 +98,10 @@ def clone(a, *arrays):
     return arrays
 
 
-def run(a, km, state, advance) -> int:
-    """The example's main loop and output for a parsed argument set (shared with the E3SM example)."""
+def run(a, km, state, advance, names=None, initial_row_times=None) -> int:
+    """The example's main loop and output for a parsed argument set (shared with the E3SM and
+    aerosol examples); names: the output columns after T (default: the gas species);
+    initial_row_times: (t, dt) written in the iter -1 row (default: tbeg and dtmax)."""
     B = state.shape[0]
     tadv = make_tadv(a, B)
     t = np.full(B, a.tbeg)
@@ -108,8 +110,10 @@ def run(a, km, state, advance) -> int:
     f = open(a.outputfile, "w") if a.write_time_profiles else None
     try:
         if f:
-            f.write(header_line(km.species_names))
-            f.write(state_lines(-1, t, dt, state))
+            f.write(header_line(km.species_names if names is None else names))
+            t0, dt0 = (t, dt) if initial_row_times is None else (np.full(B, initial_row_times[0]),
+                                                                 np.full(B, initial_row_times[1]))
+            f.write(state_lines(-1, t0, dt0, state))
         clock = [time.perf_counter()]
 
         def write(it, t_, dt_, state_):

@@ -256,3 +256,17 @@ def test_driver_timestep_reproduces_reference_output():
     assert np.all(status == 0)
     assert compare_tchem(out[:, 3:], exp[:, 3:]) <= 1e-8
     assert device_error() == 0
+
+
+@pytest.mark.parametrize("name", ["tines_batched_full_gas.npy", "tines_batched_cb_full_gas.npy"])
+def test_aerosol_example_on_the_engine(tmp_path, name):
+    """The aerosol example driver (tchem_gb.examples.aerosol_chemistry) with the reference's
+    TinesODE command line, through the engine's runHostBatch."""
+    from test_examples import tines_args
+    from tchem_gb.examples import aerosol_chemistry
+    out = tmp_path / "full_gas.dat"
+    assert aerosol_chemistry.main([*tines_args(name), f"--outputfile={out}",
+                                   f"--outputfile_times={tmp_path / 't.json'}"]) == 0
+    rows = np.genfromtxt(out, skip_header=1)
+    golden = np.load(A / name).reshape(rows.shape)
+    assert compare_tchem(rows, golden) <= 1e-8
