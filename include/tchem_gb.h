@@ -429,6 +429,14 @@ int tchem_gb_numerics_read(const char* yaml_path, tchem_gb_numerics* out);
  * at A + t*128*32, B + t*32*N, D + t*128*N; N a multiple of 16 in [16, 256]. Bounded waits report
  * through tchem_gb_device_error. Validation on a GPU is pending. */
 int tchem_gb_tc_tile_update_tf32(int ntiles, int N, const float* A, const float* B, float* D, void* stream);
+/* Blocked FP32 LU with partial pivoting of nbatch matrices A[b][m][lda] (row-major, in place),
+ * one CTA per matrix: 32-column panels on the CUDA cores (pivot: first largest magnitude in the
+ * current row order, whole-row swaps; piv[b][k] = the row swapped with row k), U12 = L11^-1 A12 on
+ * the CUDA cores, and the trailing update A22 -= L21 U12 on the tensor cores (TF32 operands, FP32
+ * accumulation in TMEM, tiles of 128 rows x up to 256 columns). info[b] = 0, k + 1 when column k
+ * has no usable pivot, -1 when a bounded wait expired. Device arrays; validation on a GPU is
+ * pending. */
+int tchem_gb_tc_lu_factor_tf32(int nbatch, int m, int lda, float* A, int32_t* piv, int32_t* info, void* stream);
 
 /* Measurement helper (no counterpart in the reference): FMA throughput of the current device in
  * FLOP/s for FP64 (fp64 = 1) or FP32, from independent FMA chains on every SM. These are the

@@ -147,6 +147,7 @@ def lib() -> C.CDLL:
         "tchem_gb_aero_rhs": (C.c_int, [vp, vp, C.c_int, vp, vp, vp, vp]),
         "tchem_gb_numerics_read": (C.c_int, [C.c_char_p, C.POINTER(Numerics)]),
         "tchem_gb_tc_tile_update_tf32": (C.c_int, [C.c_int, C.c_int, vp, vp, vp, vp]),
+        "tchem_gb_tc_lu_factor_tf32": (C.c_int, [C.c_int, C.c_int, C.c_int, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

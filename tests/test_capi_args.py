@@ -127,3 +127,8 @@ def test_tensor_core_tile_update_checks_its_shape():
         assert L.tchem_gb_tc_tile_update_tf32(1, n, nul, nul, nul, nul) == ERR_ARG
     assert L.tchem_gb_tc_tile_update_tf32(2, 64, nul, nul, nul, nul) == ERR_ARG
     assert b"null" in L.tchem_gb_last_error()
+    lu = L.tchem_gb_tc_lu_factor_tf32
+    assert lu(0, 300, 304, nul, nul, nul, nul) == 0  # no matrices
+    assert lu(1, 0, 1, nul, nul, nul, nul) == ERR_ARG
+    assert lu(1, 300, 299, nul, nul, nul, nul) == ERR_ARG  # lda < m
+    assert lu(4, 300, 304, nul, nul, nul, nul) == ERR_ARG and b"null" in L.tchem_gb_last_error()
