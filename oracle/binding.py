@@ -22,6 +22,8 @@ def load(native: bool = False) -> C.CDLL:
         vp = C.c_void_p
         L.oracle_set_lu_tile_bits.restype = C.c_int
         L.oracle_set_lu_tile_bits.argtypes = [C.c_int]
+        L.oracle_lu_factor_blocked.restype = C.c_int
+        L.oracle_lu_factor_blocked.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.oracle_kforward.restype = C.c_int
         L.oracle_kforward.argtypes = [vp, C.c_double, C.c_double, vp]
         L.oracle_reaction_rates.restype = C.c_int
@@ -298,3 +300,15 @@ def tangent(o: "Oracle", tadv, state, tol_newton, tape: Tape, dx0, dtheta, k_sca
 
 def library_path() -> Path:
     return LIB_PATH
+
+
+def lu_factor_blocked(a: np.ndarray, keep: int = 10) -> tuple[np.ndarray, np.ndarray]:
+    """(lu, piv) of the FP32 matrix a as the tensor-core LU computes it (TF32 tiles for keep = 10)."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    n = a.shape[0]
+    lu = np.zeros_like(a)
+    piv = np.zeros(n, dtype=np.int32)
+    rc = load().oracle_lu_factor_blocked(n, a.ctypes.data, int(keep), lu.ctypes.data, piv.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"oracle_lu_factor_blocked returned {rc}")
+    return lu, piv

@@ -893,6 +893,20 @@ Settings replay_settings(const tchem_gb_tadv& ta, const double* tol_newton) {
 
 extern "C" {
 
+// One FP32 matrix factored as the tensor-core LU does (DenseLU::factor_blocked with `keep`
+// mantissa bits in the trailing-update operands; 23 = no rounding): lu[n][n] holds the unit-lower
+// L below the diagonal and U on and above it, piv[k] the row swapped with row k.
+int oracle_lu_factor_blocked(int n, const float* a_in, int keep, float* lu, int32_t* piv) {
+  if (n < 1 || !a_in || !lu || !piv || keep < 1 || keep > 23) return TCHEM_GB_ERR_ARG;
+  DenseLU<float> f;
+  f.resize(n);
+  std::copy(a_in, a_in + static_cast<size_t>(n) * n, f.a.begin());
+  if (!f.factor_blocked(keep)) return TCHEM_GB_ERR_DEVICE;
+  std::copy(f.a.begin(), f.a.end(), lu);
+  for (int k = 0; k < n; ++k) piv[k] = f.piv[k];
+  return TCHEM_GB_OK;
+}
+
 int oracle_set_lu_tile_bits(int bits) {
   if (bits != 0 && (bits < 1 || bits > 23)) return TCHEM_GB_ERR_ARG;
   g_lu_tile_bits = bits;

@@ -37,6 +37,10 @@ extern "C" {
  * panels in FP32 and the trailing update with operands rounded to `bits` mantissa bits (10: TF32,
  * 7: BF16) and FP32 accumulation; 0 (default): the unblocked FP32 LU. A process-wide setting. */
 int oracle_set_lu_tile_bits(int bits);
+/* One FP32 matrix a[n][n] factored as the tensor-core LU does: 32-column panels with partial
+ * pivoting, trailing update on operands rounded to `keep` mantissa bits (10: TF32, 23: none);
+ * lu[n][n] and piv[n] as LAPACK's sgetrf (0-based pivots). */
+int oracle_lu_factor_blocked(int n, const float* a, int keep, float* lu, int32_t* piv);
 
 /* kfor[nReac] for one (T, p). */
 int oracle_kforward(const tchem_gb_kmcd_view* km, double T, double p, double* kfor);

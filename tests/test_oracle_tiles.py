@@ -43,3 +43,25 @@ def test_tile_precision_against_fp64(bits, simplified, bound):
     assert np.all(r[3] == 0)
     assert rel_error(r[0][:, 3:3 + m], ref[0][:, 3:3 + m], 1e-12).max() <= bound
     np.testing.assert_array_equal(r[4]["n_steps"], ref[4]["n_steps"])
+
+
+@pytest.mark.parametrize("keep,bound", [(23, 2e-6), (10, 5e-4)])  # measured 3.4e-7, 7.7e-5
+def test_blocked_lu_restatement_factors_the_matrix(keep, bound):
+    """The oracle's factorization in the tensor-core LU's order (the reference a GPU run of
+    tchem_gb_tc_lu_factor_tf32 is compared with): P A = L U to FP32 (keep = 23) or TF32-operand
+    (keep = 10) accuracy on a 300 x 300 Newton-like matrix I - c J, with the pivots LAPACK's
+    partial pivoting gives on the same matrix."""
+    from oracle import lu_factor_blocked
+    rng = np.random.default_rng(3)
+    n = 300
+    a = (np.eye(n) - 0.05 * rng.standard_normal((n, n))).astype(np.float32)
+    lu, piv = lu_factor_blocked(a, keep)
+    L = np.tril(lu.astype(np.float64), -1) + np.eye(n)
+    U = np.triu(lu.astype(np.float64))
+    pa = a.astype(np.float64).copy()
+    for k in range(n):
+        pa[[k, piv[k]]] = pa[[piv[k], k]]
+    assert np.abs(pa - L @ U).max() / np.abs(a).max() <= bound
+    import scipy.linalg
+    _, piv_ref = scipy.linalg.lu_factor(a.astype(np.float64))
+    assert np.mean(piv == piv_ref) > 0.95
