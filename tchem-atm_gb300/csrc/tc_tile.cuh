@@ -27,7 +27,7 @@ __host__ __device__ constexpr uint32_t kmajor_offset(int row, int k, int kw) {
 
 // Shared-memory matrix descriptor: start address, LBO, SBO (bytes, multiples of 16), fixed
 // version bits 46-48 = 0b001, base offset 0, no swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+__host__ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
   uint64_t d = static_cast<uint64_t>((saddr & 0x3FFFFu) >> 4);
   d |= static_cast<uint64_t>((lbo & 0x3FFFFu) >> 4) << 16;
   d |= static_cast<uint64_t>((sbo & 0x3FFFFu) >> 4) << 32;
