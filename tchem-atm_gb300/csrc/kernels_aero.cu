@@ -12,17 +12,12 @@
 // The Jacobian is a forward difference of the RHS, column j with the step 1e-8 max(|y_j|, 1e-20),
 // as the reference's computeJacobian (computeNumericalJacobian,
 // TChem_Impl_AerosolChemistry_Problem.hpp:204-236).
-//
-// Per sample, the temperature and pressure terms of each SIMPOL entry (accommodation coefficient,
-// mean free path, partitioning constant, kg m-3 -> ppm factor; TChem_Impl_SIMPOL_constant.hpp:50-130)
-// are evaluated once. Per RHS evaluation the lanes run over reactions (rates of progress), then over
-// particles (radius, mean molecular weight and mass; TChem_Impl_SingleParticleUtils.hpp:50-170),
-// then over (particle, entry) pairs (the transfers), and each row gathers its terms in the
-// reference's order (particles outer, entries inner), so no atomics are needed.
+// The right-hand side itself is in aero_rhs.cuh.
 #include "advance.hpp"
 #include "engine.cuh"
 #include "fp64_core.cuh"
 #include "kernels.hpp"
+#include "aero_rhs.cuh"
 
 namespace tchem_gb {
 
@@ -51,31 +46,6 @@ AeroWarpLayout aero_warp_layout(const MechLayout& L, const AeroDev& A, int lda, 
 
 namespace fp64 {
 
-constexpr double kAeroPi = 3.141592653589793;
-constexpr double kAeroRuniv = 8.314472;  // J/(mol K), src/core/TChem_Util.hpp
-constexpr double kAeroAtmPa = 101325.0;  // Pa
-
-// Everything one right-hand-side evaluation reads and writes (built once per sample, passed by
-// reference to the one out-of-line evaluation routine, which keeps the kernels small to compile).
-struct AeroEval {
-  const double* x;       // [M] ODE vector (shared memory)
-  const double* keff;    // [R]
-  double* q;             // [R] rates of progress
-  double* f;             // [M] result
-  double* simc;          // [nS][4]: accommodation coefficient, mean free path, partitioning constant, kg m-3 -> ppm
-  double* part;          // [nP][3]: radius, mean molecular weight, mass
-  double* dsim;          // [nP][nS]: cond - evap of each (particle, entry) pair
-  double* nc;            // [nP]: number concentrations of the sample
-  const int32_t* rf_ptr;
-  const int16_t* rf_sp;
-  const int32_t* pr_ptr;
-  const int16_t* pr_r;
-  const double* pr_nu;
-  const double* emis;
-  AeroDev A;
-  int32_t R;
-};
-
 // Per-sample context of the aerosol problem (the members fp64_core.cuh reads, plus the evaluation data).
 template <int NPL>
 struct AeroCtx {
@@ -101,95 +71,6 @@ __device__ __forceinline__ void publish(AeroCtx<NPL>& c, const double (&y)[NPL])
   __syncwarp();
 }
 
-// Temperature and pressure terms of every SIMPOL entry, lanes over entries.
-__device__ __forceinline__ void aero_setup(const AeroEval& E, int lane, double t, double p) {
-  const AeroDev& A = E.A;
-  for (int is = lane; is < A.nS; is += 32) {
-    const int32_t* I = A.sim_idx + 3 * is;
-    const double* P = A.sim_par + 7 * is;
-    const double B1 = P[0], B2 = P[1], B3 = P[2], B4 = P[3], D = P[4], N_star = P[5], MW = P[6];
-    double alpha = 0.1;
-    if (I[2]) {
-      const double n23 = pow(N_star, 2.0 / 3.0);
-      double dh = -10.0 * (N_star - 1.0) + 7.53 * (n23 - 1.0) - 1.0;
-      double ds = -32.0 * (N_star - 1.0) + 9.21 * (n23 - 1.0) - 1.3;
-      dh = dh * 4184.0;
-      ds = ds * 4.184;
-      const double dg = dh - t * ds;
-      alpha = exp(-dg / (kAeroRuniv * t));
-      alpha = alpha / (1.0 + alpha);
-    }
-    double vp = B1 / t + B2 + B3 * t + B4 * log(t);
-    vp = kAeroAtmPa * pow(10.0, vp);
-    double* sc = E.simc + 4 * is;
-    sc[0] = alpha;
-    sc[1] = 3.0 * D / sqrt(8.0 * kAeroRuniv * t / (kAeroPi * MW));
-    sc[2] = vp / p / MW * 1.0e6;
-    sc[3] = kAeroRuniv / MW * 1.0e6 * t / p;
-  }
-}
-
-// E.f = RHS at the ODE vector in E.x; called by the whole warp, ends with a warp barrier.
-__device__ __noinline__ void aero_eval(const AeroEval& E, int lane) {
-  const AeroDev& A = E.A;
-  const double* x = E.x;
-  const int mg = A.m_gas, nA = A.nA, nS = A.nS, nP = A.nP, M = A.M;
-  for (int r = lane; r < E.R; r += 32) {
-    double q = E.keff[r];
-    for (int g = E.rf_ptr[r]; g < E.rf_ptr[r + 1]; ++g) q *= x[E.rf_sp[g]];
-    E.q[r] = q;
-  }
-  for (int ip = lane; ip < nP; ip += 32) {
-    const double* xp = x + mg + ip * nA;
-    double volume = A.vol0, mass = A.mass0, moles = A.moles0;
-    for (int k = 0; k < nA; ++k) volume += xp[k] / A.density[k];
-    for (int k = 0; k < nA; ++k) {
-      mass += xp[k];
-      moles += xp[k] / A.mw[k];
-    }
-    E.part[3 * ip] = pow(volume * 3.0 / 4.0 / kAeroPi, 1.0 / 3.0);
-    E.part[3 * ip + 1] = mass / moles;
-    E.part[3 * ip + 2] = mass;
-  }
-  __syncwarp();
-  for (int e = lane; e < nP * nS; e += 32) {
-    const int ip = e / nS, is = e - ip * nS;
-    const int aero = A.sim_idx[3 * is] + ip * nA, gas = A.sim_idx[3 * is + 1];
-    const double* sc = E.simc + 4 * is;
-    const double alpha = sc[0], mfp = sc[1], keq = sc[2];
-    const double D = A.sim_par[7 * is + 4];
-    const double radius = E.part[3 * ip], avg_mw = E.part[3 * ip + 1], mass = E.part[3 * ip + 2];
-    const double kn = mfp / radius;
-    const double ffs = (0.75 * alpha * (1.0 + kn)) / (kn * kn + (1.0 + 0.283 * alpha) * kn + 0.75 * alpha);
-    double cond = 4.0 * kAeroPi * radius * D * ffs;
-    double evap = cond * 1.0 * (keq * avg_mw / mass);
-    // the host admits gas in [0, m_gas) and aero in [m_gas, M) only; the guards keep reads in bounds
-    cond *= (gas >= 0 && gas < mg) ? x[gas] : 0.0;
-    evap *= (aero >= mg && aero < M) ? x[aero] : 0.0;
-    E.dsim[e] = -evap + cond;
-  }
-  __syncwarp();
-  for (int i = lane; i < M; i += 32) {
-    double acc = 0.0;
-    if (i < mg) {
-      acc = E.emis[i];
-      for (int e = E.pr_ptr[i]; e < E.pr_ptr[i + 1]; ++e) acc += E.pr_nu[e] * E.q[E.pr_r[e]];
-      bool any = false;
-      for (int is = 0; is < nS; ++is) any |= A.sim_idx[3 * is + 1] == i;
-      if (any)
-        for (int ip = 0; ip < nP; ++ip)
-          for (int is = 0; is < nS; ++is)
-            if (A.sim_idx[3 * is + 1] == i) acc += -E.nc[ip] * E.dsim[ip * nS + is];
-    } else {
-      const int ip = (i - mg) / nA;
-      for (int is = 0; is < nS; ++is)
-        if (A.sim_idx[3 * is] + ip * nA == i) acc += E.dsim[ip * nS + is] / E.simc[4 * is + 3];
-    }
-    E.f[i] = acc;
-  }
-  __syncwarp();
-}
-
 template <int NPL>
 __device__ __forceinline__ void fetch_f(const AeroCtx<NPL>& c, double (&f)[NPL]) {
 #pragma unroll
@@ -202,7 +83,7 @@ __device__ __forceinline__ void fetch_f(const AeroCtx<NPL>& c, double (&f)[NPL])
 template <int NPL>
 __device__ __forceinline__ void rhs(AeroCtx<NPL>& c, const double (&y)[NPL], double (&f)[NPL]) {
   publish(c, y);
-  aero_eval(c.E, c.lane);
+  aero_eval<32>(c.E, c.lane);
   fetch_f(c, f);
   __syncwarp();
   ++c.st.n_rhs;
@@ -213,7 +94,7 @@ template <int NPL>
 __device__ __forceinline__ void newton_matrix(AeroCtx<NPL>& c, const double (&y)[NPL], double coef) {
   publish(c, y);
   double f0[NPL];
-  aero_eval(c.E, c.lane);
+  aero_eval<32>(c.E, c.lane);
   fetch_f(c, f0);
   const int M = c.E.A.M, lda = c.lda;
   double* A = c.W.A;
@@ -226,7 +107,7 @@ __device__ __forceinline__ void newton_matrix(AeroCtx<NPL>& c, const double (&y)
     __syncwarp();
     if (c.lane == 0) x[j] = yh;
     __syncwarp();
-    aero_eval(c.E, c.lane);
+    aero_eval<32>(c.E, c.lane);
 #pragma unroll
     for (int k = 0; k < NPL; ++k) {
       const int i = c.lane + 32 * k;
@@ -320,7 +201,7 @@ __global__ void __launch_bounds__(256, 1) aero_kernel(const __grid_constant__ Ae
     const double p = row[1], Tk = row[2];
     compute_keff(P.mech, P.mech.rate_param, Tk, p, row + 3 + mg, W.keff, lane);
     for (int ip = lane; ip < P.aero.nP; ip += 32) E.nc[ip] = P.number_conc[static_cast<size_t>(s) * P.aero.nP + ip];
-    aero_setup(E, lane, Tk, p);
+    aero_setup<32>(E, lane, Tk, p);
     __syncwarp();
     AeroCtx<NPL> c{W, lane, P.lda, tchem_gb_sample_stats{}, E};
     double y[NPL];
