@@ -15,9 +15,7 @@ def load(native: bool = False) -> C.CDLL:
     """The oracle library: the accuracy reference, or (native) the host-tuned build timed as the
     CPU baseline."""
     if native not in _libs:
-        path = NATIVE_LIB_PATH if native else LIB_PATH
-        if not path.exists():
-            build(native=native)
+        path = build(native=native)  # rebuilt when missing or older than its sources
         L = C.CDLL(str(path))
         vp = C.c_void_p
         L.oracle_set_lu_tile_bits.restype = C.c_int
