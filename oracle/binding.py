@@ -6,7 +6,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .build import LIB_PATH, NATIVE_LIB_PATH, build
+from .build import LIB_PATH, build
 
 _libs: dict = {}
 
