@@ -115,9 +115,10 @@ struct Driver {
       check_cuda(cudaMemcpy(status.data(), d_status, sizeof(int32_t) * B, cudaMemcpyDeviceToHost), "cudaMemcpy");
       check_cuda(cudaMemcpy(stats.data(), d_stats, sizeof(tchem_gb_sample_stats) * B, cudaMemcpyDeviceToHost),
                  "cudaMemcpy");
-      bool done = true;
+      bool done = true, advanced = false;
       for (size_t b = 0; b < B; ++b) {
         if (status[b] == TCHEM_GB_SAMPLE_SKIPPED) continue;
+        if (status[b] == TCHEM_GB_SAMPLE_OK && t[b] > tadv[b].tbeg) advanced = true;
         total[b].n_steps += stats[b].n_steps;
         total[b].n_rejected += stats[b].n_rejected;
         total[b].n_newton_fail += stats[b].n_newton_fail;
@@ -134,7 +135,7 @@ struct Driver {
         if (dt[b] > 0.0) tadv[b].dt = dt[b];
         if (t[b] < del_t) done = false;
       }
-      if (done) break;
+      if (done || !advanced) break;  // every row at del_t, or a call that moved no row forward
     }
     int32_t derr = 0;
     check(tchem_gb_device_error(d_ws, nullptr, &derr), "tchem_gb_device_error");
