@@ -86,6 +86,9 @@ def parse() -> argparse.Namespace:
                     help="samples of the discrete-adjoint leg (1800 s horizon, FP64); 0 skips it")
     ap.add_argument("--e3sm-samples", type=int, default=65536,
                     help="samples of the E3SM leg (the reference's 80-column uci scenario tiled); 0 skips it")
+    ap.add_argument("--tc-lu-matrices", type=int, default=0,
+                    help="matrices of the tensor-core LU leg (300 x 300 FP32, TF32 trailing updates on tcgen05): "
+                         "factorizations/s and the TF32 rate of the trailing updates; 0 skips it")
     ap.add_argument("--aerosol-samples", type=int, default=0,
                     help="samples of the gas-aerosol (SIMPOL.1) leg: the reference driver test's CB05CL_AE5 + SOA "
                          "sample perturbed, one 30 s driver time step (83 ODEs, plain FP64); 0 skips it")
@@ -536,6 +539,44 @@ def aerosol_leg(B: int, cpu_seconds: float, dev, stream) -> dict:
                                        f"over samples on {cores} threads ({el:.2f} s)"}}
 
 
+# ---- tensor-core LU (300-species factorization) -----------------------------------------------
+
+def tc_lu_leg(nb: int, dev, stream) -> dict:
+    """Batched 300 x 300 FP32 LU with TF32 trailing updates on the tensor cores
+    (tchem_gb_tc_lu_factor_tf32, one CTA per matrix), the factorization of the 300-species
+    mechanism's Newton matrices: factorizations/s, the trailing-update TF32 flops per second
+    (sum over panels of 2 (m - p1)^2 * 32) and the factors against the oracle's restatement on the
+    first matrix."""
+    import torch
+    from oracle import lu_factor_blocked
+    from tchem_gb.tensor_core import lu_factor_tf32
+    n, lda = 300, 304
+    rng = np.random.default_rng(5)
+    a = (np.eye(n) - 0.05 * rng.standard_normal((nb, n, n))).astype(np.float32)
+    A0 = np.zeros((nb, n, lda), np.float32)
+    A0[:, :, :n] = a
+    d0 = torch.from_numpy(A0).to(dev)
+    dA = d0.clone()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    lu_factor_tf32(dA, stream=stream)
+    torch.cuda.synchronize(dev)
+    best = float("inf")
+    for _ in range(3):
+        dA.copy_(d0)
+        ev[0].record(stream)
+        piv, info = lu_factor_tf32(dA, stream=stream)
+        ev[1].record(stream)
+        torch.cuda.synchronize(dev)
+        best = min(best, ev[0].elapsed_time(ev[1]))
+    upd = sum(2.0 * (n - p1) ** 2 * 32 for p1 in range(32, n, 32))
+    ref_lu, ref_piv = lu_factor_blocked(a[0], keep=10)
+    lu0 = dA[0, :, :n].cpu().numpy()
+    return {"matrices": nb, "m": n, "ms": best, "factorizations_per_s": nb / (best * 1e-3),
+            "trailing_update_tflops": nb * upd / (best * 1e-3) / 1e12, "info_ok": int((info == 0).sum().item()),
+            "vs_oracle": {"pivots_equal": bool(np.array_equal(piv[0].cpu().numpy(), ref_piv)),
+                          "max_rel_factor_diff": float(np.abs(lu0 - ref_lu).max() / np.abs(ref_lu).max())}}
+
+
 # ---- discrete adjoint -------------------------------------------------------------------------
 
 def adjoint_leg(km, state, tol_time, n: int, dev, stream) -> dict:
@@ -742,6 +783,9 @@ def engine_arm(args, world: int, rank: int, local: int):
 
     if rank == 0 and args.e3sm_samples > 0:
         line["e3sm"] = e3sm_leg(args.e3sm_samples, min(args.cpu_seconds, 5.0), dev, stream)
+
+    if rank == 0 and args.tc_lu_matrices > 0:
+        line["tc_lu"] = tc_lu_leg(args.tc_lu_matrices, dev, stream)
 
     if rank == 0 and args.aerosol_samples > 0:
         line["aerosol"] = aerosol_leg(args.aerosol_samples, min(args.cpu_seconds, 5.0), dev, stream)
