@@ -86,6 +86,9 @@ def parse() -> argparse.Namespace:
                     help="samples of the discrete-adjoint leg (1800 s horizon, FP64); 0 skips it")
     ap.add_argument("--e3sm-samples", type=int, default=65536,
                     help="samples of the E3SM leg (the reference's 80-column uci scenario tiled); 0 skips it")
+    ap.add_argument("--large-samples", type=int, default=0,
+                    help="samples of the 300-species / 1000-reaction leg in the plain FP64 form (the baseline the "
+                         "tensor-core factorization is compared with), 10 s horizon; 0 skips it")
     ap.add_argument("--tc-lu-matrices", type=int, default=0,
                     help="matrices of the tensor-core LU leg (300 x 300 FP32, TF32 trailing updates on tcgen05): "
                          "factorizations/s and the TF32 rate of the trailing updates; 0 skips it")
@@ -539,6 +542,44 @@ def aerosol_leg(B: int, cpu_seconds: float, dev, stream) -> dict:
                                        f"over samples on {cores} threads ({el:.2f} s)"}}
 
 
+# ---- 300-species mechanism, plain FP64 ---------------------------------------------------------
+
+def large_leg(B: int, dev, stream) -> dict:
+    """The seeded 300-species / 1000-reaction mechanism (the large dense-LU configuration: same rate
+    mix, at most 2 reactants and 4 products) in the plain FP64 form, B samples over 10 s (a short
+    horizon of the 3600 s configuration, which the plain form would take hours to cover at this
+    size); the first 2 end states against the FP64 oracle."""
+    import torch
+    from oracle import Oracle
+    from tchem_gb import AtmosphericChemistry, tadv_to_device, time_advance_array
+    km = KineticModel.from_string(mechanism_yaml(MechanismSpec(n_species=300, n_reactions=1000, seed=20251205)))
+    m = km.n_active
+    state = sample_states(B, m, seed=SEED + 21)
+    tadv = time_advance_array(B, tend=10.0, dt=1e-10, dtmin=1e-10, dtmax=10.0, max_num_newton_iterations=20,
+                              num_time_iterations_per_interval=10**7)
+    tol_time = np.tile([ATOL, RTOL], (m, 1))
+    d = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+    d_state, d_tadv, d_tt = d(state), tadv_to_device(tadv, dev), d(tol_time)
+    d_tn = torch.tensor(TOL_NEWTON, dtype=torch.float64, device=dev)
+    out = torch.empty_like(d_state)
+    t = torch.zeros(B, dtype=torch.float64, device=dev)
+    dt = torch.zeros_like(t)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ev[0].record(stream)
+    status = AtmosphericChemistry.runDeviceBatch(d_tn, d_tt, None, d_tadv, d_state, t, dt, out, km, form="plain",
+                                                 stream=stream)
+    ev[1].record(stream)
+    torch.cuda.synchronize(dev)
+    ms = ev[0].elapsed_time(ev[1])
+    K = min(2, B)
+    ref = Oracle([km], native=True).time_advance(tadv[:K], state[:K], TOL_NEWTON, tol_time)[0]
+    res = out[:K].cpu().numpy()
+    err = rel_err(res[:, 3:3 + m], ref[:, 3:3 + m])
+    return {"samples": B, "species": m, "reactions": km.nReac, "horizon_s": 10.0, "form": "plain", "ms": ms,
+            "value": B / (ms * 1e-3), "unit": "samples/s", "status_ok": int((status == 0).sum().item()),
+            "max_rel_err_vs_oracle": float(err.max())}
+
+
 # ---- tensor-core LU (300-species factorization) -----------------------------------------------
 
 def tc_lu_leg(nb: int, dev, stream) -> dict:
@@ -783,6 +824,9 @@ def engine_arm(args, world: int, rank: int, local: int):
 
     if rank == 0 and args.e3sm_samples > 0:
         line["e3sm"] = e3sm_leg(args.e3sm_samples, min(args.cpu_seconds, 5.0), dev, stream)
+
+    if rank == 0 and args.large_samples > 0:
+        line["large_mechanism"] = large_leg(args.large_samples, dev, stream)
 
     if rank == 0 and args.tc_lu_matrices > 0:
         line["tc_lu"] = tc_lu_leg(args.tc_lu_matrices, dev, stream)
