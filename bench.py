@@ -1,26 +1,30 @@
 #!/usr/bin/env python3
 """Benchmark of the batched box-model TR-BDF2 time advance (TChem::AtmosphericChemistry::runDeviceBatch).
 
-Workload (one "step"): advance every sample of the CB05-shaped batch -- 51 active species, one
-constant species, 156 reactions (60 % Arrhenius, 10 % Troe, 30 % fixed-J photolysis), seeded --
-from t = 0 to the 3600 s horizon with adaptive TR-BDF2 steps (dt_in = dt_min = 1e-10, dt_max =
-3600, atol 1e-12, rtol 1e-6, Newton 1e-18 / 1e-8, at most 20 Newton iterations). The batch is
-1,048,576 samples per GPU with T ~ U[260, 310] K, p ~ U[0.8, 1.05] atm and number densities
-log-uniform in [1e2, 1e12] cm^-3 (synthetic, seeded). The state array (1,048,576 x 55 doubles,
-461 MB) is larger than L2, so no flush is needed between steps.
+Workload: the CB05-shaped batch -- 51 active species, one constant species, 156 reactions (60 %
+Arrhenius, 10 % Troe, 30 % fixed-J photolysis), seeded -- advanced from t = 0 to the 3600 s horizon
+with adaptive TR-BDF2 steps (dt_in = dt_min = 1e-10, dt_max = 3600, atol 1e-12, rtol 1e-6, Newton
+1e-18 / 1e-8, at most 20 Newton iterations). 1,048,576 samples per GPU with T ~ U[260, 310] K,
+p ~ U[0.8, 1.05] atm and number densities log-uniform in [1e2, 1e12] cm^-3 (synthetic, seeded). The
+state array (1,048,576 x 55 doubles, 461 MB) is larger than L2, so no flush is needed between steps.
+
+The timed loop is the reference's host time loop (src/examples/TChem_AtmosphericChemistry.cpp:312-352):
+every "step" is one runDeviceBatch call over the whole batch followed by the carry-over of t and dt
+into the time-advance records (one device kernel, tchem_gb_time_advance_carry_over). Each call
+advances every sample by at most S steps (num_time_iterations_per_interval; S = the probe's mean step
+count / K), the last of the K calls without that limit, so the K timed steps take every sample from
+t = 0 to the horizon. The W warm-up steps run the same calls on a separate copy of the batch.
 
 Metric: box-samples/s = samples advanced to the horizon per second (whole job, all ranks).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference] [--form simplified]
 
---impl engine (default) times the engine's chosen form through the device API (value), then one
-end-to-end pass through the host-buffer C ABI with host<->device copies inside the timed region
-(e2e), the plain FP64 form on a subsample, the CPU oracle on a bounded subsample (cpu_baseline)
-and the end-state error of the chosen form against the FP64 results.
-The E3SM leg ("e3sm") times AtmosphericChemistryE3SM::runDeviceBatch on the reference's
-80-column uci scenario (photolysis rates and external forcing as per-sample inputs) in the three
-forms, the NetProductionRates kernel, the CPU restatement on the host cores, and checks the end
-states against the reference's golden.
+--impl engine (default) times the chosen form through the device API (value); the same K calls through
+the host-buffer C ABI with the host<->device copies of every call inside the timed region (e2e); the
+plain FP64 form and the other mixed form on subsamples, with the chosen form's end-state error against
+the plain FP64 results; the CPU oracle on a bounded subsample (cpu_baseline, and the error against the
+FP64 oracle); and the side legs: the uneven batch in one graph launch, the discrete adjoint, the
+E3SM scenario, the gas-aerosol driver case and the 300-species mechanism.
 --impl reference times the reference algorithm's CPU restatement (the oracle, FP64, OpenMP on all
 host threads) on a bounded subsample per step; the reference's own Kokkos build cannot be built
 here (Kokkos, Tines, Sacado and yaml-cpp are absent).
@@ -32,6 +36,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import subprocess
 import sys
@@ -54,35 +59,35 @@ HORIZON = 3600.0
 TOL_NEWTON = (1e-18, 1e-8)
 ATOL, RTOL = 1e-12, 1e-6
 SEED = 7
+UNCAPPED = 10_000_000  # step budget of a call that runs every sample to its horizon
 # Form names of the C ABI's tchem_gb_form.
 FORM_DTYPE = {"plain": "f64", "mixed": "f64 state / f32 LU + f64-residual refinement",
               "simplified": "f64 state / f32 Gauss-Jordan inverse"}
-# DRAM bytes per sample of the simplified-form kernel in the autotuned two-warp shape, from one ncu
-# capture of a 4096-sample, 600 s case (profiles/trbdf2_simplified_2warp_cb05_4096.md: 2,656,512
-# bytes read, 0 written -- the results were still in L2 when the capture ended). The per-sample
-# traffic (state, time-advance record and times read once) does not depend on the horizon, so it
-# scales by samples.
+# DRAM bytes per sample of the time-advance kernel, from one ncu capture of a 4096-sample case of
+# the same kernel (dram__bytes_read.sum + dram__bytes_write.sum over the launch, divided by the
+# samples). The per-sample traffic (state, time-advance record and times read once, results written
+# once) does not depend on the horizon or on the batch size, so it scales by samples.
 NCU_DRAM_BYTES_PER_SAMPLE = {"simplified": 2656512 / 4096}
 
 
 def parse() -> argparse.Namespace:
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=1)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20, help="timed runDeviceBatch calls that take the batch to the horizon")
+    ap.add_argument("--warmup", type=int, default=5, help="untimed calls on a separate copy of the batch")
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
     ap.add_argument("--form", choices=["simplified", "mixed", "plain"], default="simplified")
     ap.add_argument("--samples", type=int, default=1 << 20, help="samples per GPU (the workload is 1,048,576)")
-    ap.add_argument("--plain-samples", type=int, default=4096, help="subsample for the plain FP64 form")
+    ap.add_argument("--plain-samples", type=int, default=16384, help="subsample for the plain FP64 form")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of one oracle sample")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--other-samples", type=int, default=65536,
                     help="subsample for the other mixed form (mixed <-> simplified)")
-    ap.add_argument("--uneven-samples", type=int, default=0,
+    ap.add_argument("--uneven-samples", type=int, default=262144,
                     help="samples of the uneven-batch leg (262144 in the reference's uneven configuration): 75 %% on "
                          "the 51-species and 25 %% on a 120-species mechanism, half night, horizons 600/1800/3600 s, "
                          "autotuned shapes, one CUDA-graph launch; 0 skips it")
-    ap.add_argument("--adjoint-samples", type=int, default=8192,
+    ap.add_argument("--adjoint-samples", type=int, default=65536,
                     help="samples of the discrete-adjoint leg (1800 s horizon, FP64); 0 skips it")
     ap.add_argument("--e3sm-samples", type=int, default=65536,
                     help="samples of the E3SM leg (the reference's 80-column uci scenario tiled); 0 skips it")
@@ -92,7 +97,7 @@ def parse() -> argparse.Namespace:
     ap.add_argument("--tc-lu-matrices", type=int, default=0,
                     help="matrices of the tensor-core LU leg (300 x 300 FP32, TF32 trailing updates on tcgen05): "
                          "factorizations/s and the TF32 rate of the trailing updates; 0 skips it")
-    ap.add_argument("--aerosol-samples", type=int, default=0,
+    ap.add_argument("--aerosol-samples", type=int, default=65536,
                     help="samples of the gas-aerosol (SIMPOL.1) leg: the reference driver test's CB05CL_AE5 + SOA "
                          "sample perturbed, one 30 s driver time step (83 ODEs, plain FP64); 0 skips it")
     return ap.parse_args()
@@ -246,7 +251,7 @@ def run_oracle(km, state, tadv, tol_time, n: int):
 
 def bench_config(B: int, form: str, world: int) -> dict:
     """The workload description shared by both arms."""
-    return {"workload": f"cb05-shaped 51 species / 156 reactions, {B} samples per GPU, 3600 s TR-BDF2",
+    return {"workload": f"cb05-shaped 51 species / 156 reactions, {B} samples per GPU, 0 -> 3600 s TR-BDF2",
             "samples_per_gpu": B, "horizon_s": HORIZON, "form": form, "parallelism": f"replicas x{world}",
             "l2": "inputs larger than L2 (461 MB state per GPU); no flush"}
 
@@ -289,8 +294,9 @@ def reference_arm(args, world: int, rank: int):
 
 # ---- uneven batch -------------------------------------------------------------------------------
 
-def uneven_leg(B: int, dev, stream) -> dict:
-    """Mixed mechanism sizes, day/night variants and three horizons in one graph-captured launch."""
+def uneven_leg(B: int, form: str, dev, stream) -> dict:
+    """Mixed mechanism sizes, day/night variants and three horizons in one graph-captured launch,
+    in the chosen form; end states of a stratified subsample against the plain FP64 form."""
     import torch
     from tchem_gb import AtmosphericChemistry, tadv_to_device
     spec120 = MechanismSpec(n_species=120, n_reactions=330, seed=20251204)
@@ -323,8 +329,8 @@ def uneven_leg(B: int, dev, stream) -> dict:
         km = mechs[k]
         tps, times = AtmosphericChemistry.autotune(km, d_tn, d_tt[:km.n_active], tadv_to_device(tadv[sel], dev),
                                                    torch.as_tensor(state[sel][:, :km.state_dim]).to(dev),
-                                                   form="simplified", stream=stream)
-        AtmosphericChemistry.set_threads_per_sample(mechs[k + 1], tps)
+                                                   form=form, stream=stream)
+        AtmosphericChemistry.set_threads_per_sample(mechs[k + 1], tps, form=form)
         tuned[f"{km.n_active}_species"] = {"threads_per_sample": tps,
                                            "probe_ms": {str(a): round(b, 1) for a, b in times.items()}}
     d_state = torch.as_tensor(state).to(dev)
@@ -332,7 +338,7 @@ def uneven_leg(B: int, dev, stream) -> dict:
     t = torch.zeros(B, dtype=torch.float64, device=dev)
     dt = torch.zeros_like(t)
     g, status = AtmosphericChemistry.capture(d_tn, d_tt, tadv_to_device(tadv, dev), d_state, t, dt, out, mechs,
-                                             mech_of_sample=torch.as_tensor(mos).to(dev), form="simplified")
+                                             mech_of_sample=torch.as_tensor(mos).to(dev), form=form)
     g.replay()  # warm-up replay (the capture helper also ran the batch once eagerly)
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -341,11 +347,28 @@ def uneven_leg(B: int, dev, stream) -> dict:
     e1.record()
     torch.cuda.synchronize(dev)
     ms = e0.elapsed_time(e1)
-    return {"samples": B, "value": B / (ms * 1e-3), "unit": "samples/s", "ms": ms,
-            "failed_samples": int((status != 0).sum()),
+    res = out.cpu().numpy()
+    # accuracy: 512 samples of each 51-species variant and 64 of each 120-species variant against the
+    # plain FP64 form (one call per mechanism)
+    acc = {}
+    for k, n in ((0, 512), (1, 512), (2, 64), (3, 64)):
+        sel = np.nonzero(mos == k)[0][:n]
+        km = mechs[k]
+        st = torch.as_tensor(state[sel][:, :km.state_dim]).to(dev)
+        po = torch.empty_like(st)
+        pt = torch.zeros(len(sel), dtype=torch.float64, device=dev)
+        pdt = torch.zeros_like(pt)
+        AtmosphericChemistry.runDeviceBatch(d_tn, d_tt[:km.n_active], None, tadv_to_device(tadv[sel], dev), st, pt,
+                                            pdt, po, km, form="plain", stream=stream)
+        ref = po.cpu().numpy()[:, 3:3 + km.n_active]
+        e = rel_err(res[sel][:, 3:3 + km.n_active], ref)
+        acc[f"{km.n_active}_species_{'night' if k % 2 else 'day'}"] = {"samples": len(sel), "max": float(e.max()),
+                                                                        "p99": float(np.percentile(e, 99))}
+    return {"samples": B, "value": B / (ms * 1e-3), "unit": "samples/s", "ms": ms, "form": form,
+            "failed_samples": int((status.cpu().numpy() != 0).sum()),
             "mix": {"51_species": int((~big).sum()), "120_species": int(big.sum()), "night": int(night.sum())},
             "launch": "one CUDA graph (t reset, bucketing, one persistent kernel per mechanism structure)",
-            "autotuned": tuned}
+            "autotuned": tuned, "accuracy_vs_plain_fp64_gpu": acc}
 
 
 # ---- E3SM gas chemistry -----------------------------------------------------------------------
@@ -442,8 +465,8 @@ def e3sm_leg(B: int, cpu_seconds: float, dev, stream) -> dict:
             "net_production_rates": {"value": B / (ms_rates * 1e-3), "unit": "samples/s", "ms": ms_rates,
                                      "achieved_gbs": rate_bytes / (ms_rates * 1e-3) / 1e9,
                                      "bytes_per_sample": rate_bytes // B, "bound": "fp64",
-                                     "profile": "profiles/e3sm_rates_uci_col_262144.md: FP64 pipe 86.6 % of "
-                                                "peak, DRAM 0.2 % (262,144 samples)"},
+                                     "profile": "ncu of this kernel on 262,144 samples: FP64 pipe 86.6 % of "
+                                                "peak, DRAM 0.2 %"},
             "accuracy_vs_reference_golden": acc,
             "cpu_baseline": {"value": n / el, "unit": "samples/s", "cores": cores, "kind": "port",
                              "sample": f"first {n} samples, E3SM CPU restatement built for the host CPU, OpenMP over "
@@ -666,127 +689,197 @@ def adjoint_leg(km, state, tol_time, n: int, dev, stream) -> dict:
 
 # ---- engine arm -------------------------------------------------------------------------------
 
+class HostLoop:
+    """The reference's host time loop over one batch on the device: runDeviceBatch calls with the
+    carry-over of t and dt between them, each call advancing every sample by the step budget that
+    the previous carry-over wrote (caps_for). Arrays are private copies, so the caller's inputs stay
+    untouched; the state advances in place (state_out = state), as in the reference's example."""
+
+    def __init__(self, km, form, d_tn, d_tt, tadv: np.ndarray, d_state0, first_cap: int, stats: bool, dev):
+        import torch
+        from tchem_gb import AtmosphericChemistry, tadv_to_device
+        self.AC = AtmosphericChemistry
+        self.km, self.form, self.d_tn, self.d_tt = km, form, d_tn, d_tt
+        t0 = tadv.copy()
+        t0["num_time_iterations_per_interval"] = first_cap
+        self.tadv = tadv_to_device(t0, dev)
+        self.state = d_state0.clone()
+        B = d_state0.shape[0]
+        self.t = torch.zeros(B, dtype=torch.float64, device=dev)
+        self.dt = torch.zeros_like(self.t)
+        self.status = torch.empty(B, dtype=torch.int32, device=dev)
+        self.stats = torch.zeros(B, 8, dtype=torch.int32, device=dev) if stats else None
+        self.total = torch.zeros(B, 8, dtype=torch.int64, device=dev) if stats else None
+        self.ws = torch.empty(AtmosphericChemistry.getWorkSpaceSize(km, B, form=form), dtype=torch.uint8, device=dev)
+
+    def advance(self, stream):
+        """One runDeviceBatch call (the time-advance kernel)."""
+        self.AC.runDeviceBatch(self.d_tn, self.d_tt, None, self.tadv, self.state, self.t, self.dt, self.state, self.km,
+                               status=self.status, stats=self.stats, form=self.form, workspace=self.ws, stream=stream)
+
+    def carry(self, stream, next_cap: int):
+        """The carry-over of t and dt, with the next call's step budget."""
+        if self.total is not None:
+            self.total += self.stats
+        self.AC.carry_over(self.tadv, self.t, self.dt, next_cap, stream=stream)
+
+
+def caps_for(K: int, cap: int) -> list[int]:
+    """Step budgets of the K calls: `cap` for calls 1..K-1, none for the last."""
+    return [cap] * (K - 1) + [UNCAPPED]
+
+
 def engine_arm(args, world: int, rank: int, local: int):
     import torch
-    from tchem_gb import AtmosphericChemistry, tadv_to_device
+    from tchem_gb import AtmosphericChemistry, kernel_launches, tadv_to_device
 
     assert torch.cuda.is_available(), "the engine arm needs a CUDA device"
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    B = args.samples
+    B, K, W = args.samples, max(1, args.steps), max(0, args.warmup)
     km, state, tadv, tol_time = workload(B, rank)
     m = km.n_active
     stream = torch.cuda.current_stream(dev)
+    L = _capi.lib()
 
     d_tn = torch.tensor(TOL_NEWTON, dtype=torch.float64, device=dev)
     d_tt = torch.as_tensor(tol_time).to(dev)
     d_tadv = tadv_to_device(tadv, dev)
     d_state = torch.as_tensor(state).to(dev)
-    d_out = torch.empty_like(d_state)
-    d_t = torch.zeros(B, dtype=torch.float64, device=dev)
-    d_dt = torch.zeros_like(d_t)
-    d_status = torch.empty(B, dtype=torch.int32, device=dev)
-    d_stats = torch.zeros(B, 8, dtype=torch.int32, device=dev)
+
+    # probe: the autotuner picks the kernel shape (threads per sample) on the first 4096 samples over
+    # the full horizon; one more probe run gives the mean step count that sizes the per-call budget
+    P0 = min(4096, B)
     tuned = None
     if args.form != "plain":
-        # the autotuner picks the kernel shape (threads per sample) on a probe of the batch
-        P0 = min(4096, B)
         tps, times = AtmosphericChemistry.autotune(km, d_tn, d_tt, d_tadv[:P0], d_state[:P0].contiguous(),
                                                    form=args.form, stream=stream)
         tuned = {"threads_per_sample": tps, "probe_samples": P0,
                  "probe_ms": {str(a): round(b, 1) for a, b in times.items()}}
-    ws_bytes = AtmosphericChemistry.getWorkSpaceSize(km, B, form=args.form)
-    d_ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    p_out = torch.empty(P0, d_state.shape[1], dtype=torch.float64, device=dev)
+    p_t = torch.zeros(P0, dtype=torch.float64, device=dev)
+    p_dt = torch.zeros_like(p_t)
+    p_stats = torch.zeros(P0, 8, dtype=torch.int32, device=dev)
+    AtmosphericChemistry.runDeviceBatch(d_tn, d_tt, None, d_tadv[:P0], d_state[:P0].contiguous(), p_t, p_dt, p_out,
+                                        km, stats=p_stats, form=args.form, stream=stream)
+    ps = p_stats.cpu().numpy()
+    probe_iters = float((ps[:, 0] + ps[:, 1] + ps[:, 2]).mean())
+    cap = max(1, math.ceil(probe_iters / K))
+    caps = caps_for(K, cap)
 
-    def step(with_stats: bool):
-        d_t.zero_()  # every sample restarts at t = 0 (samples with t >= tend are skipped)
-        AtmosphericChemistry.runDeviceBatch(d_tn, d_tt, None, d_tadv, d_state, d_t, d_dt, d_out, km,
-                                            status=d_status, stats=d_stats if with_stats else None,
-                                            form=args.form, workspace=d_ws, stream=stream)
-
-    for _ in range(args.warmup):
-        step(False)
+    # warm-up: W calls of the same loop (the first W budgets) on a separate copy of the batch
+    if W > 0:
+        warm = HostLoop(km, args.form, d_tn, d_tt, tadv, d_state, caps[0], False, dev)
+        for k in range(W):
+            warm.advance(stream)
+            warm.carry(stream, caps[k + 1] if k + 1 < K else UNCAPPED)
+        torch.cuda.synchronize(dev)
+        assert AtmosphericChemistry.device_error(warm.ws, stream) == 0
+        del warm
+    loop = HostLoop(km, args.form, d_tn, d_tt, tadv, d_state, caps[0], True, dev)
     torch.cuda.synchronize(dev)
-    assert AtmosphericChemistry.device_error(d_ws, stream) == 0
 
-    # timed region: K steps, CUDA events on the launching stream, barrier + sync on both sides
+    # timed region: K calls + carry-overs, CUDA events on the launching stream, barrier + sync on
+    # both sides; per-call events around the time-advance kernel alone give the roofline's launch time
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     barrier(world)
     torch.cuda.synchronize(dev)
+    n_launch0 = kernel_launches()
     with ClockSampler(local) as clk:
         e0.record(stream)
-        for k in range(args.steps):
-            step(k == args.steps - 1)
+        for k in range(K):
+            ev[k][0].record(stream)
+            loop.advance(stream)
+            ev[k][1].record(stream)
+            loop.carry(stream, caps[k + 1] if k + 1 < K else cap)
         e1.record(stream)
         torch.cuda.synchronize(dev)
+    n_launch = kernel_launches() - n_launch0
     barrier(world)
     ms_local = e0.elapsed_time(e1)
     ms = max_over_ranks(ms_local, world, dev)
-    value = B * world * args.steps / (ms * 1e-3)
-    status = d_status.cpu().numpy()
-    stats = d_stats.cpu().numpy()
-    out = d_out.cpu().numpy()
-    n_fail = int((status != 0).sum())
-    kernel_ms = ms_local / args.steps  # one engine kernel per step (one mechanism group)
+    value = B * world / (ms * 1e-3)
+    call_ms = [a.elapsed_time(b) for a, b in ev]
+    kernel_ms = sum(call_ms)
+    status = loop.status.cpu().numpy()
+    t_end = loop.t.cpu().numpy()
+    stats = loop.total.cpu().numpy()
+    out = loop.state.cpu().numpy()
+    n_fail = int((status != 0).sum()) - int((status == 2).sum())  # skipped samples finished in an earlier call
+    at_horizon = int((t_end >= HORIZON).sum())
+    assert AtmosphericChemistry.device_error(loop.ws, stream) == 0
 
-    # roofline of the time-advance kernel: algorithmic flops per launch / launch time
+    # roofline of the time-advance kernel: algorithmic flops over all K launches / their summed time
     f32, f64 = work_flops(km, stats)
     peak64, peak32 = C.c_double(), C.c_double()
-    L = _capi.lib()
     L.tchem_gb_measure_fma_peak(1, 4, 4096, C.byref(peak64))
     L.tchem_gb_measure_fma_peak(0, 4, 65536, C.byref(peak32))
     ach64 = f64 / (kernel_ms * 1e-3) / 1e12
     ach32 = f32 / (kernel_ms * 1e-3) / 1e12
     per_sample = NCU_DRAM_BYTES_PER_SAMPLE.get(args.form)
-    traffic = None if per_sample is None else per_sample * B
+    traffic = None if per_sample is None else per_sample * B / K
 
     line = {
-        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": FORM_DTYPE[args.form], "data": "synthetic (seeded CB05-shaped mechanism and states)",
-        "config": {**bench_config(B, args.form, world), "autotuned": tuned},
+        "config": {**bench_config(B, args.form, world), "autotuned": tuned,
+                   "host_loop": {"calls": K, "steps_per_call": cap, "last_call": "uncapped",
+                                 "probe_mean_step_attempts": probe_iters,
+                                 "pattern": "runDeviceBatch + carry-over of t and dt per call, in place "
+                                            "(state_out = state), as the reference's box-model example"}},
+        "samples_at_horizon": at_horizon,
         "failed_samples": n_fail,
+        "ms_per_call": [round(x, 1) for x in call_ms],
         "work_per_sample": {k: float(stats[:, i].mean()) for i, k in enumerate(
             ["steps", "rejected", "newton_fail", "newton_iter", "factorizations", "solves", "rhs", "jacobians"])},
-        "gpu_launches": args.steps,
+        "gpu_launches": n_launch,
         "clocks": clk.summary(),
         "roofline": {"bound": "fp64", "achieved": ach64, "peak": peak64.value / 1e12, "unit": "TFLOP/s",
                      "frac": ach64 / (peak64.value / 1e12), "traffic": traffic,
+                     "kernel_ms": kernel_ms, "launches": K,
                      "peak_source": "FMA-chain probe measured in this run (tchem_gb_measure_fma_peak); "
                                     "MEASURED_PEAKS.json has no FP64/FP32 figure",
+                     "traffic_source": "DRAM bytes per sample from one ncu capture of a 4096-sample case of this "
+                                       "kernel, times the samples of one launch",
                      "fp32": {"achieved": ach32, "peak": peak32.value / 1e12,
                               "frac": ach32 / (peak32.value / 1e12)},
-                     "note": "algorithmic FP64 flops count the right-hand sides only (the work formula); the FP64 "
-                             "pipe is 61 % busy in ncu for the two-warp simplified kernel "
-                             "(profiles/trbdf2_simplified_2warp_cb05_4096.md): residuals, updates, conversions "
-                             "and step control add to it; the kernel is latency-bound (issue 45 %)"},
+                     "note": "algorithmic FP64 flops count the right-hand sides only (the work formula); "
+                             "the FP32 side counts factorizations, solves and Jacobians"},
     }
 
     if rank == 0:
-        # plain FP64 form on a subsample: its rate and the FP64 end states for the error figure
+        # plain FP64 form on a subsample (one uncapped call: its trajectory is that of the K calls, since
+        # the plain form carries nothing between calls but t, dt and the state): its rate and the FP64
+        # end states for the error figure
         P = min(args.plain_samples, B)
+        pl_out = None
         if P > 0 and args.form != "plain":
-            p_out = torch.empty(P, d_state.shape[1], dtype=torch.float64, device=dev)
-            p_t = torch.zeros(P, dtype=torch.float64, device=dev)
-            p_dt = torch.zeros_like(p_t)
+            pl_out = torch.empty(P, d_state.shape[1], dtype=torch.float64, device=dev)
+            pl_t = torch.zeros(P, dtype=torch.float64, device=dev)
+            pl_dt = torch.zeros_like(pl_t)
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             ev0.record(stream)
-            st_p = AtmosphericChemistry.runDeviceBatch(d_tn, d_tt, None, d_tadv[:P], d_state[:P].contiguous(), p_t,
-                                                       p_dt, p_out, km, form="plain", stream=stream)
+            st_p = AtmosphericChemistry.runDeviceBatch(d_tn, d_tt, None, d_tadv[:P], d_state[:P].contiguous(), pl_t,
+                                                       pl_dt, pl_out, km, form="plain", stream=stream)
             ev1.record(stream)
             torch.cuda.synchronize(dev)
             plain_rate = P / (ev0.elapsed_time(ev1) * 1e-3)
-            e = rel_err(out[:P, 3:3 + m], p_out.cpu().numpy()[:, 3:3 + m])
+            pl = pl_out.cpu().numpy()
+            e = rel_err(out[:P, 3:3 + m], pl[:, 3:3 + m])
             line["plain_fp64"] = {"value": plain_rate, "unit": "samples/s", "samples": P,
                                   "failed_samples": int((st_p != 0).sum()),
+                                  "speedup_of_chosen_form": value / plain_rate,
                                   "note": "subsample of the same batch; samples are independent"}
             line["accuracy_vs_plain_fp64_gpu"] = {"samples": P, "max": float(e.max()),
                                                   "p99": float(np.percentile(e, 99)), "floor": ATOL,
-                                                  "share_at_or_below_1e-6": float(np.mean(e <= 1e-6))}
+                                                  "share_at_or_below_1e-6": float(np.mean(e <= 1e-6)),
+                                                  "bound": 1e-6}
             # the other mixed form on a subsample, with its accuracy against the same FP64 results
             other = "mixed" if args.form == "simplified" else "simplified"
             Q = min(args.other_samples, B)
-            if Q > 0 and args.form != "plain":
+            if Q > 0:
                 tps_o, _ = AtmosphericChemistry.autotune(km, d_tn, d_tt, d_tadv[:min(4096, Q)],
                                                          d_state[:min(4096, Q)].contiguous(), form=other,
                                                          stream=stream)
@@ -798,11 +891,12 @@ def engine_arm(args, world: int, rank: int, local: int):
                                                            q_dt, q_out, km, form=other, stream=stream)
                 ev1.record(stream)
                 torch.cuda.synchronize(dev)
-                eq = rel_err(q_out[:P].cpu().numpy()[:, 3:3 + m], p_out.cpu().numpy()[:, 3:3 + m])
+                R = min(P, Q)
+                eq = rel_err(q_out[:R].cpu().numpy()[:, 3:3 + m], pl[:R, 3:3 + m])
                 line[f"form_{other}"] = {"value": Q / (ev0.elapsed_time(ev1) * 1e-3), "unit": "samples/s",
                                          "samples": Q, "dtype": FORM_DTYPE[other], "threads_per_sample": tps_o,
                                          "failed_samples": int((st_q != 0).sum()),
-                                         "accuracy_vs_plain_fp64_gpu": {"samples": P, "max": float(eq.max()),
+                                         "accuracy_vs_plain_fp64_gpu": {"samples": R, "max": float(eq.max()),
                                                                         "p99": float(np.percentile(eq, 99)),
                                                                         "floor": ATOL}}
         # CPU oracle: baseline rate and the accuracy reference
@@ -811,62 +905,77 @@ def engine_arm(args, world: int, rank: int, local: int):
         e = rel_err(out[:n, 3:3 + m], res[0][:, 3:3 + m])
         cores = os.cpu_count() or 1
         line["cpu_baseline"] = {"value": n / el, "unit": "samples/s", "cores": cores, "kind": "port",
-                                "sample": f"first {n} samples of the batch, FP64 TR-BDF2 CPU restatement built for the host CPU, OpenMP "
-                                          f"over samples on {cores} threads ({el:.1f} s)"}
+                                "sample": f"first {n} samples of the batch, 0 -> 3600 s, FP64 TR-BDF2 CPU restatement "
+                                          f"built for the host CPU, OpenMP over samples on {cores} threads ({el:.1f} s)"}
         line["accuracy_vs_fp64_oracle"] = {"samples": n, "max": float(e.max()), "p99": float(np.percentile(e, 99)),
                                            "floor": ATOL}
+        if pl_out is not None:
+            eo = rel_err(pl[:min(n, P), 3:3 + m], res[0][:min(n, P), 3:3 + m])
+            line["plain_fp64"]["accuracy_vs_fp64_oracle"] = {"samples": min(n, P), "max": float(eo.max()),
+                                                             "bound": 1e-8}
 
-    if rank == 0 and args.uneven_samples > 0:
-        line["uneven_batch"] = uneven_leg(args.uneven_samples, dev, stream)
-
-    if rank == 0 and args.adjoint_samples > 0:
-        line["adjoint"] = adjoint_leg(km, state, tol_time, args.adjoint_samples, dev, stream)
-
-    if rank == 0 and args.e3sm_samples > 0:
-        line["e3sm"] = e3sm_leg(args.e3sm_samples, min(args.cpu_seconds, 5.0), dev, stream)
-
-    if rank == 0 and args.large_samples > 0:
-        line["large_mechanism"] = large_leg(args.large_samples, dev, stream)
-
-    if rank == 0 and args.tc_lu_matrices > 0:
-        line["tc_lu"] = tc_lu_leg(args.tc_lu_matrices, dev, stream)
-
-    if rank == 0 and args.aerosol_samples > 0:
-        line["aerosol"] = aerosol_leg(args.aerosol_samples, min(args.cpu_seconds, 5.0), dev, stream)
+    legs = [("uneven_batch", args.uneven_samples, lambda n: uneven_leg(n, args.form, dev, stream)),
+            ("adjoint", args.adjoint_samples, lambda n: adjoint_leg(km, state, tol_time, n, dev, stream)),
+            ("e3sm", args.e3sm_samples, lambda n: e3sm_leg(n, min(args.cpu_seconds, 5.0), dev, stream)),
+            ("large_mechanism", args.large_samples, lambda n: large_leg(n, dev, stream)),
+            ("tc_lu", args.tc_lu_matrices, lambda n: tc_lu_leg(n, dev, stream)),
+            ("aerosol", args.aerosol_samples, lambda n: aerosol_leg(n, min(args.cpu_seconds, 5.0), dev, stream))]
+    for key, n, fn in legs:
+        if rank == 0 and n > 0:
+            t0 = time.perf_counter()
+            line[key] = fn(n)
+            line[key]["leg_wall_s"] = round(time.perf_counter() - t0, 1)
 
     if not args.no_e2e:
-        # end to end through the host-buffer C ABI: pinned host arrays in, results out, every copy
-        # inside the timed region
-        h_state = torch.empty(state.shape, dtype=torch.float64, pin_memory=True).numpy()
-        h_state[:] = state
-        h_out = torch.empty(state.shape, dtype=torch.float64, pin_memory=True).numpy()
-        h_tadv = torch.empty(tadv.nbytes, dtype=torch.uint8, pin_memory=True).numpy().view(tadv.dtype)
-        h_tadv[:] = tadv
-        h_t = torch.zeros(B, dtype=torch.float64, pin_memory=True).numpy()
-        h_dt = torch.zeros(B, dtype=torch.float64, pin_memory=True).numpy()
-        h_st = torch.zeros(B, dtype=torch.int32, pin_memory=True).numpy()
-        tn = np.asarray(TOL_NEWTON, dtype=np.float64)
-        o = _capi.AdvanceOpts()
-        o.form = {"plain": 0, "mixed": 1, "simplified": 2}[args.form]
-        p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
-        handles = (C.c_void_p * 1)(km.handle.value)
-        barrier(world)
-        t0 = time.perf_counter()
-        rc = L.tchem_gb_time_advance_hostbuf(handles, 1, None, B, p(tn), p(tol_time), p(h_tadv), p(h_state),
-                                             p(h_t), p(h_dt), p(h_out), p(h_st), None, C.byref(o),
-                                             C.c_void_p(stream.cuda_stream))
-        el = time.perf_counter() - t0
-        _capi.check(rc, "tchem_gb_time_advance_hostbuf")
-        el = max_over_ranks(el, world, dev)
-        dim = state.shape[1]
-        h2d = 16 + 16 * m + tadv.itemsize * B + 8 * B * dim + 8 * B
-        d2h = 8 * B * dim + 8 * B + 8 * B + 4 * B
-        line["e2e"] = {"value": B * world / el, "unit": "samples/s", "h2d_bytes_per_step": h2d,
-                       "d2h_bytes_per_step": d2h, "failed_samples": int((h_st != 0).sum()),
-                       "path": "tchem_gb_time_advance_hostbuf (C ABI, pinned host buffers)"}
-        line["gpu_launches"] = args.steps  # the e2e pass is timed separately
+        line["e2e"] = e2e_loop(km, state, tadv, tol_time, args.form, K, cap, world, dev, stream)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def e2e_loop(km, state, tadv, tol_time, form: str, K: int, cap: int, world: int, dev, stream) -> dict:
+    """The same K-call host loop end to end through the host-buffer C ABI
+    (tchem_gb_time_advance_hostbuf, the runHostBatch face): pinned host arrays in, every call copies
+    its inputs to the device and its results back, the carry-over of t and dt runs on the host
+    between calls (as in the reference's loop over runHostBatch)."""
+    import torch
+    B, dim, m = state.shape[0], state.shape[1], km.n_active
+    pin = lambda shape, dt: torch.empty(shape, dtype=dt, pin_memory=True).numpy()  # noqa: E731
+    h_state = pin(state.shape, torch.float64)
+    h_state[:] = state
+    h_tadv = pin((tadv.nbytes,), torch.uint8).view(tadv.dtype)
+    h_tadv[:] = tadv
+    h_t = pin((B,), torch.float64)
+    h_t[:] = 0.0
+    h_dt = pin((B,), torch.float64)
+    h_st = pin((B,), torch.int32)
+    tn = np.asarray(TOL_NEWTON, dtype=np.float64)
+    o = _capi.AdvanceOpts()
+    o.form = {"plain": 0, "mixed": 1, "simplified": 2}[form]
+    p = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    handles = (C.c_void_p * 1)(km.handle.value)
+    caps = caps_for(K, cap)
+    L = _capi.lib()
+    h_tadv["num_time_iterations_per_interval"] = caps[0]
+    barrier(world)
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    for k in range(K):
+        rc = L.tchem_gb_time_advance_hostbuf(handles, 1, None, B, p(tn), p(tol_time), p(h_tadv), p(h_state),
+                                             p(h_t), p(h_dt), p(h_state), p(h_st), None, C.byref(o),
+                                             C.c_void_p(stream.cuda_stream))
+        _capi.check(rc, "tchem_gb_time_advance_hostbuf")
+        h_tadv["tbeg"] = h_t
+        h_tadv["dt"] = h_dt
+        h_tadv["num_time_iterations_per_interval"] = caps[k + 1] if k + 1 < K else cap
+    el = time.perf_counter() - t0
+    el = max_over_ranks(el, world, dev)
+    h2d = 16 + 16 * m + tadv.itemsize * B + 8 * B * dim + 8 * B
+    d2h = 8 * B * dim + 8 * B + 8 * B + 4 * B
+    return {"value": B * world / el, "unit": "samples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "steps": K, "samples_at_horizon": int((h_t >= HORIZON).sum()),
+            "failed_samples": int(((h_st != 0) & (h_st != 2)).sum()),
+            "path": "tchem_gb_time_advance_hostbuf per call (C ABI, pinned host buffers, copies inside the timed "
+                    "region), host-side carry-over of t and dt"}
 
 
 def main():

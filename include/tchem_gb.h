@@ -280,10 +280,17 @@ int tchem_gb_time_advance_hostbuf(const tchem_gb_mech* const* mechs, int n_mechs
  * inside the library (held by every device context that loads it). The mechanisms' device tables
  * must already exist on the current device (call tchem_gb_workspace_bytes with them once at
  * set-up); calls needing more scratch than 1 MiB (batches mixing mechanism structures need 4 bytes
- * per sample and group) are rejected with TCHEM_GB_ERR_ARG. The first call on a device looks up
- * the array's address: make it before any stream capture. All calls share the array: calls that
- * overlap on the GPU race and must be serialised. Device-side wait timeouts are not reported
- * through tchem_gb_device_error; samples no kernel reached keep the caller's status value. */
+ * per sample and group) are rejected with TCHEM_GB_ERR_ARG; a mechanism outside the path gives
+ * TCHEM_GB_ERR_UNSUPPORTED, as tchem_gb_time_advance does. That set-up call also looks up the
+ * array's device address, which loads the module holding it (and so places its 1 MiB) on the
+ * current device; without it, the first call of this entry point on a device does the lookup
+ * itself and may allocate then. CUDA also places a kernel's code on the device at its first
+ * launch (lazy module loading, the default): callers that must see no allocation at all include one
+ * tchem_gb_time_advance call with the same mechanisms and form in their set-up (or run with
+ * CUDA_MODULE_LOADING=EAGER). Make the set-up calls before any stream capture. All calls share
+ * the array: calls that overlap on the GPU race and must be serialised. Device-side wait timeouts
+ * are not reported through tchem_gb_device_error; samples no kernel reached keep the caller's
+ * status value. */
 int tchem_gb_time_advance_noalloc(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample,
                                   int nbatch, const double* tol_newton, const double* tol_time, const double* fac,
                                   const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
@@ -337,6 +344,19 @@ int tchem_gb_mech_set_threads_per_sample(tchem_gb_mech* mech, int form, int thre
 /* Synchronizes `stream`, then reads and clears the device error word of `workspace` (NULL: the
  * library-owned workspace). *device_error is 0 when no kernel reported a timed-out wait. */
 int tchem_gb_device_error(void* workspace, void* stream, int32_t* device_error);
+
+/* The carry-over step of the reference's host time loop between two tchem_gb_time_advance calls
+ * (the parallel_reduce of src/examples/TChem_AtmosphericChemistry.cpp:340-350): for every sample
+ * tadv[i].tbeg = t_out[i] and tadv[i].dt = dt_out[i]; when iters_per_interval > 0 it also sets
+ * tadv[i].num_time_iterations_per_interval (the step budget of the next call); when t_sum is not
+ * NULL, *t_sum = sum of t_out (the loop's stopping test is mean t >= 0.9999 tend). Device arrays,
+ * stream-ordered, one kernel launch. */
+int tchem_gb_time_advance_carry_over(tchem_gb_tadv* tadv, const double* t_out, const double* dt_out, int nbatch,
+                                     int iters_per_interval, double* t_sum, void* stream);
+
+/* Number of kernels the library has launched in this process (every entry point counts each
+ * launch it made). No counterpart in the reference; for benchmarks and tests. */
+long long tchem_gb_kernel_launches(void);
 
 /* Unit entry points on device arrays (state[nbatch][nSpec+3]):
  *   kfor[nbatch][nReac] rate constants, omega[nbatch][m] net production rates (active species),

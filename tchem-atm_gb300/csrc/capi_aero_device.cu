@@ -273,6 +273,7 @@ int tchem_gb_aero_time_advance(const tchem_gb_mech* mech, const tchem_gb_aero* a
   P.error_word = reinterpret_cast<int32_t*>(ws + 64);
   e = launch_aero(P, false, plan.grid, plan.warps, plan.smem, stream);
   if (e != cudaSuccess) return cuda_fail(e, "aerosol time-advance kernel launch");
+  note_launch();
   return TCHEM_GB_OK;
 }
 
@@ -316,6 +317,7 @@ int tchem_gb_aero_rhs(const tchem_gb_mech* mech, const tchem_gb_aero* aero, int 
   P.error_word = reinterpret_cast<int32_t*>(ws + 64);
   cudaError_t e = launch_aero(P, true, plan.grid, plan.warps, plan.smem, stream);
   if (e != cudaSuccess) return cuda_fail(e, "aerosol RHS kernel launch");
+  note_launch();
   return TCHEM_GB_OK;
 }
 

@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <mutex>
 #include <stdexcept>
@@ -81,6 +82,12 @@ int fail(int code, const std::string& msg) {
 int cuda_fail(cudaError_t e, const char* where) {
   return fail(TCHEM_GB_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
+
+namespace {
+std::atomic<long long> g_kernel_launches{0};
+}  // namespace
+
+void note_launch(int n) { g_kernel_launches.fetch_add(n, std::memory_order_relaxed); }
 
 namespace {
 
@@ -229,6 +236,23 @@ void fill_slots(const GroupPlan& g, const tchem_gb_mech* const* mechs, int dev, 
 
 }  // namespace
 
+int workspace_bytes_checked(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch,
+                            const tchem_gb_advance_opts* opts, size_t* bytes) {
+  *bytes = 0;
+  try {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    *bytes = make_plan(mechs, n_mechs, nbatch, n_mechs > 1, opts_or_default(opts), dev).bytes;
+    return TCHEM_GB_OK;
+  } catch (const std::domain_error& e) {
+    return fail(TCHEM_GB_ERR_UNSUPPORTED, e.what());
+  } catch (const std::bad_alloc&) {
+    return fail(TCHEM_GB_ERR_NOMEM, "tchem_gb_workspace_bytes: allocation failed");
+  } catch (const std::exception& e) {
+    return fail(TCHEM_GB_ERR_ARG, e.what());
+  }
+}
+
 }  // namespace tchem_gb
 
 using namespace tchem_gb;
@@ -237,15 +261,12 @@ extern "C" {
 
 size_t tchem_gb_workspace_bytes(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch,
                                 const tchem_gb_advance_opts* opts) {
-  try {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    const Plan p = make_plan(mechs, n_mechs, nbatch, n_mechs > 1, opts_or_default(opts), dev);
-    return p.bytes;
-  } catch (const std::exception& e) {
-    set_last_error(e.what());
-    return 0;
-  }
+  size_t bytes = 0;
+  if (workspace_bytes_checked(mechs, n_mechs, nbatch, opts, &bytes) != TCHEM_GB_OK) return 0;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  noalloc_setup(dev);  // set-up time: load the fixed scratch of tchem_gb_time_advance_noalloc
+  return bytes;
 }
 
 }  // extern "C"
@@ -326,6 +347,7 @@ int time_advance_impl(const tchem_gb_mech* const* mechs, int n_mechs, const int3
       for (int gm : plan.groups[g].mechs) G.group_of_mech[gm] = static_cast<int32_t>(g);
     e = launch_bucket(mech_of_sample, nbatch, G, n_mechs, counts, items, status, stream);
     if (e != cudaSuccess) return cuda_fail(e, "bucket kernel");
+    note_launch();
   }
   for (size_t g = 0; g < plan.groups.size(); ++g) {
     const GroupPlan& gp = plan.groups[g];
@@ -371,6 +393,7 @@ int time_advance_impl(const tchem_gb_mech* const* mechs, int n_mechs, const int3
     else
       e = launch_trbdf2_fp64(P, gp.grid, gp.warps_per_block, gp.smem, stream);
     if (e != cudaSuccess) return cuda_fail(e, "time-advance kernel launch");
+    note_launch();
   }
   return TCHEM_GB_OK;
 }
@@ -534,6 +557,7 @@ int tchem_gb_adjoint(const tchem_gb_mech* mech, int nbatch, const double* tol_ne
   P.error_word = reinterpret_cast<int32_t*>(ws + 64);
   e = launch_adjoint(P, a.grid, a.warps, a.smem, stream);
   if (e != cudaSuccess) return cuda_fail(e, "adjoint kernel launch");
+  note_launch();
   return TCHEM_GB_OK;
 }
 
@@ -600,6 +624,8 @@ int tchem_gb_autotune(tchem_gb_mech* mech, int form, int nbatch, const double* t
   *chosen = best;
   return TCHEM_GB_OK;
 }
+
+long long tchem_gb_kernel_launches(void) { return g_kernel_launches.load(std::memory_order_relaxed); }
 
 int tchem_gb_device_error(void* workspace, void* stream_v, int32_t* device_error) {
   if (!device_error) return fail(TCHEM_GB_ERR_ARG, "tchem_gb_device_error: null argument");
@@ -668,6 +694,7 @@ int run_unit(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech
   P.status = nullptr;
   cudaError_t e = launch_unit(P, kind, static_cast<cudaStream_t>(stream_v));
   if (e != cudaSuccess) return cuda_fail(e, "unit kernel launch");
+  note_launch();
   return TCHEM_GB_OK;
 }
 
@@ -814,6 +841,7 @@ int run_e3sm_rates(const tchem_gb_mech* mech, int nbatch, const double* state, c
   P.out = out;
   const cudaError_t e = launch_e3sm(P, kind, device_info(dev).sm_count, static_cast<cudaStream_t>(stream_v));
   if (e != cudaSuccess) return cuda_fail(e, who);
+  note_launch();
   return TCHEM_GB_OK;
 }
 
@@ -918,6 +946,7 @@ int tchem_gb_e3sm_time_advance(const tchem_gb_mech* mech, int nbatch, const doub
   E.out = keff;
   cudaError_t e = launch_e3sm(E, E3SM_KEFF, device_info(dev).sm_count, stream);
   if (e != cudaSuccess) return cuda_fail(e, "E3SM rate-constant kernel launch");
+  note_launch();
   RateArgs ra;
   ra.keff = keff;
   if (external_sources) {

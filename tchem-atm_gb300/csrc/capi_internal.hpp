@@ -33,4 +33,17 @@ void* owned_workspace_peek(int dev);
 int fail(int code, const std::string& msg);
 int cuda_fail(cudaError_t e, const char* where);
 
+// Adds n to the library's count of kernel launches (tchem_gb_kernel_launches); called by every
+// entry point after each launch that was accepted.
+void note_launch(int n = 1);
+
+// tchem_gb_workspace_bytes with the error code kept (TCHEM_GB_ERR_UNSUPPORTED for a mechanism
+// outside the path, TCHEM_GB_ERR_ARG for bad arguments); *bytes = 0 on error.
+int workspace_bytes_checked(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch,
+                            const tchem_gb_advance_opts* opts, size_t* bytes);
+
+// Resolves the device address of tchem_gb_time_advance_noalloc's fixed scratch on device dev
+// (loading the module that holds it); returns false when the lookup failed.
+bool noalloc_setup(int dev);
+
 }  // namespace tchem_gb

@@ -17,8 +17,12 @@
 //  * The mechanisms' device tables must already be on the current device: call
 //    tchem_gb_workspace_bytes (or any other time-advance entry point) once at set-up, where
 //    allocation is allowed. Otherwise the call is rejected with TCHEM_GB_ERR_ARG.
-//  * The first call on each device looks up the scratch array's device address
-//    (cudaGetSymbolAddress); make that first call before any stream capture.
+//  * The scratch array's device address is looked up once per device (cudaGetSymbolAddress),
+//    which loads the module that holds the array and so allocates its 1 MiB then (CUDA loads
+//    modules lazily by default). tchem_gb_workspace_bytes does this lookup at set-up for the
+//    current device; a first call of this entry point on a device where nothing did it does
+//    the lookup itself, and may therefore allocate once. Make the set-up call (or that first
+//    call) before any stream capture.
 //  * Every call on a device shares the one scratch array, which keeps the last call's contents.
 //    Each call clears the parts that must start at zero (queue heads, error word, group counts)
 //    on its stream before its kernels run. Calls that overlap on the GPU (other streams, other
@@ -32,6 +36,7 @@
 #include <string>
 #include <vector>
 
+#include "capi_internal.hpp"
 #include "mech_host.hpp"
 
 namespace {
@@ -45,7 +50,31 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratch
 std::mutex g_noalloc_mu;
 std::vector<void*> g_noalloc_ptr;  // device address of g_noalloc_scratch per device ordinal
 
+// The device address of the scratch on device dev (looked up on first use); nullptr and *err set
+// when the lookup fails.
+void* scratch_address(int dev, cudaError_t* err) {
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (static_cast<int>(g_noalloc_ptr.size()) <= dev) g_noalloc_ptr.resize(dev + 1, nullptr);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    *err = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (*err != cudaSuccess || !p) return nullptr;
+    g_noalloc_ptr[dev] = p;
+  }
+  *err = cudaSuccess;
+  return g_noalloc_ptr[dev];
+}
+
 }  // namespace
+
+namespace tchem_gb {
+bool noalloc_setup(int dev) {
+  cudaError_t e = cudaSuccess;
+  if (scratch_address(dev, &e)) return true;
+  cudaGetLastError();  // a failed lookup here is reported by the entry point's own call
+  return false;
+}
+}  // namespace tchem_gb
 
 extern "C" int tchem_gb_time_advance_noalloc(const tchem_gb_mech* const* mechs, int n_mechs,
                                              const int32_t* mech_of_sample, int nbatch, const double* tol_newton,
@@ -80,25 +109,15 @@ extern "C" int tchem_gb_time_advance_noalloc(const tchem_gb_mech* const* mechs, 
       return TCHEM_GB_ERR_ARG;
     }
   }
-  // Set-up once per device, with that device current: the scratch array's device address.
-  void* scratch = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (static_cast<int>(g_noalloc_ptr.size()) <= dev) g_noalloc_ptr.resize(dev + 1, nullptr);
-    if (!g_noalloc_ptr[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p) {
-        set_last_error(std::string("tchem_gb_time_advance_noalloc: cudaGetSymbolAddress: ") +
-                       cudaGetErrorString(e));
-        return TCHEM_GB_ERR_CUDA;
-      }
-      g_noalloc_ptr[dev] = p;
-    }
-    scratch = g_noalloc_ptr[dev];
+  // The scratch array's device address on this device (looked up once, with the device current).
+  void* scratch = scratch_address(dev, &e);
+  if (!scratch) {
+    set_last_error(std::string("tchem_gb_time_advance_noalloc: cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    return TCHEM_GB_ERR_CUDA;
   }
-  const size_t need = tchem_gb_workspace_bytes(mechs, n_mechs, nbatch, opts);
-  if (need == 0) return TCHEM_GB_ERR_ARG;  // message set by tchem_gb_workspace_bytes
+  size_t need = 0;
+  const int rc = tchem_gb::workspace_bytes_checked(mechs, n_mechs, nbatch, opts, &need);
+  if (rc != TCHEM_GB_OK) return rc;  // same code and message as tchem_gb_time_advance
   if (need > kNoAllocScratchBytes) {
     set_last_error("tchem_gb_time_advance_noalloc: this call needs " + std::to_string(need) +
                    " bytes of scratch but the fixed scratch holds " + std::to_string(kNoAllocScratchBytes) +

@@ -287,6 +287,7 @@ extern "C" int tchem_gb_tc_lu_factor_tf32(int nbatch, int m, int lda, float* A, 
                                                                          reinterpret_cast<int32_t*>(ws + 64));
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "tc_lu_kernel launch");
+  note_launch();
   return TCHEM_GB_OK;
 }
 
@@ -316,5 +317,6 @@ extern "C" int tchem_gb_tc_tile_update_tf32(int ntiles, int N, const float* A, c
       N, ncols, A, B, D, reinterpret_cast<int32_t*>(ws + 64));
   e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "tc_tile_update_kernel launch");
+  note_launch();
   return TCHEM_GB_OK;
 }

@@ -11,4 +11,5 @@ AerosolChemistry, AerosolRHS).
 from .mechanism import (KineticModel, scenario_batch_size, set_scenario_conditions,  # noqa: F401
                         set_scenario_external_forcing, set_scenario_photolysis_rates)
 from .atmospheric_chemistry import (  # noqa: F401
-    AtmosphericChemistry, jacobian, kforward, reaction_rates, tadv_to_device, time_advance_array)
+    AtmosphericChemistry, jacobian, kernel_launches, kforward, reaction_rates, tadv_to_device,
+    time_advance_array)

@@ -123,6 +123,8 @@ def lib() -> C.CDLL:
         "tchem_gb_time_advance_hostbuf": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp,
                                                     vp, vp, popts, vp]),
         "tchem_gb_device_error": (C.c_int, [vp, vp, C.POINTER(C.c_int32)]),
+        "tchem_gb_time_advance_carry_over": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, vp, vp]),
+        "tchem_gb_kernel_launches": (C.c_longlong, []),
         "tchem_gb_kforward": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp]),
         "tchem_gb_reaction_rates": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp]),
         "tchem_gb_jacobian": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp]),

@@ -210,6 +210,16 @@ class AtmosphericChemistry:
         return g, status
 
     @staticmethod
+    def carry_over(tadv, t_out, dt_out, iters_per_interval: int = 0, t_sum=None, stream=None):
+        """The host loop's carry-over between two runDeviceBatch calls
+        (src/examples/TChem_AtmosphericChemistry.cpp:340-350): tadv.tbeg = t_out, tadv.dt = dt_out
+        per sample, the next call's step budget when iters_per_interval > 0, and the sum of t_out
+        into t_sum (a float64 CUDA tensor of one element) when given. One kernel on the stream."""
+        rc = _capi.lib().tchem_gb_time_advance_carry_over(_ptr(tadv), _ptr(t_out), _ptr(dt_out), int(t_out.shape[0]),
+                                                          int(iters_per_interval), _ptr(t_sum), _stream_ptr(stream))
+        _capi.check(rc, "tchem_gb_time_advance_carry_over")
+
+    @staticmethod
     def device_error(workspace=None, stream=None) -> int:
         err = C.c_int32(0)
         _capi.check(_capi.lib().tchem_gb_device_error(_ptr(workspace), _stream_ptr(stream), C.byref(err)),
@@ -249,3 +259,8 @@ def jacobian(kmcd, state, out=None, **kw):
     out = out if out is not None else torch.empty(state.shape[0], km.n_active, km.n_active, dtype=torch.float64,
                                                   device=state.device)
     return _unit("tchem_gb_jacobian", kmcd, state, out, **kw)
+
+
+def kernel_launches() -> int:
+    """Kernels the engine library has launched in this process (tchem_gb_kernel_launches)."""
+    return int(_capi.lib().tchem_gb_kernel_launches())
