@@ -54,6 +54,7 @@ from tchem_gb import _capi  # noqa: E402
 from tchem_gb.generator import MechanismSpec, mechanism_yaml, sample_states  # noqa: E402
 from tchem_gb.mechanism import KineticModel  # noqa: E402
 
+T_START = time.perf_counter()
 METRIC = "box-samples/s"
 HORIZON = 3600.0
 TOL_NEWTON = (1e-18, 1e-8)
@@ -61,13 +62,13 @@ ATOL, RTOL = 1e-12, 1e-6
 SEED = 7
 UNCAPPED = 10_000_000  # step budget of a call that runs every sample to its horizon
 # Form names of the C ABI's tchem_gb_form.
-FORM_DTYPE = {"plain": "f64", "mixed": "f64 state / f32 LU + f64-residual refinement",
+FORM_DTYPE = {"plain": "f64", "mixed": "f64 state / f32 Gauss-Jordan inverse or LU + f64-residual refinement",
               "simplified": "f64 state / f32 Gauss-Jordan inverse"}
 # DRAM bytes per sample of the time-advance kernel, from one ncu capture of a 4096-sample case of
 # the same kernel (dram__bytes_read.sum + dram__bytes_write.sum over the launch, divided by the
 # samples). The per-sample traffic (state, time-advance record and times read once, results written
 # once) does not depend on the horizon or on the batch size, so it scales by samples.
-NCU_DRAM_BYTES_PER_SAMPLE = {"simplified": 2656512 / 4096}
+NCU_DRAM_BYTES_PER_SAMPLE: dict[str, float] = {}
 
 
 def parse() -> argparse.Namespace:
@@ -76,7 +77,9 @@ def parse() -> argparse.Namespace:
     ap.add_argument("--steps", type=int, default=20, help="timed runDeviceBatch calls that take the batch to the horizon")
     ap.add_argument("--warmup", type=int, default=5, help="untimed calls on a separate copy of the batch")
     ap.add_argument("--impl", choices=["engine", "reference"], default="engine")
-    ap.add_argument("--form", choices=["simplified", "mixed", "plain"], default="simplified")
+    ap.add_argument("--form", choices=["simplified", "mixed", "plain"], default="mixed",
+                    help="mixed (default): full Newton with an FP32 Gauss-Jordan inverse or LU and FP64-residual "
+                         "refinement; simplified: simplified Newton on a carried FP32 inverse; plain: FP64 LU")
     ap.add_argument("--samples", type=int, default=1 << 20, help="samples per GPU (the workload is 1,048,576)")
     ap.add_argument("--plain-samples", type=int, default=16384, help="subsample for the plain FP64 form")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="target CPU time of one oracle sample")
@@ -97,7 +100,9 @@ def parse() -> argparse.Namespace:
     ap.add_argument("--tc-lu-matrices", type=int, default=0,
                     help="matrices of the tensor-core LU leg (300 x 300 FP32, TF32 trailing updates on tcgen05): "
                          "factorizations/s and the TF32 rate of the trailing updates; 0 skips it")
-    ap.add_argument("--aerosol-samples", type=int, default=65536,
+    ap.add_argument("--leg-budget-s", type=float, default=1000.0,
+                    help="side legs start only while the run's wall time is below this (seconds)")
+    ap.add_argument("--aerosol-samples", type=int, default=8192,
                     help="samples of the gas-aerosol (SIMPOL.1) leg: the reference driver test's CB05CL_AE5 + SOA "
                          "sample perturbed, one 30 s driver time step (83 ODEs, plain FP64); 0 skips it")
     return ap.parse_args()
@@ -767,9 +772,11 @@ def engine_arm(args, world: int, rank: int, local: int):
     cap = max(1, math.ceil(probe_iters / K))
     caps = caps_for(K, cap)
 
-    # warm-up: W calls of the same loop (the first W budgets) on a separate copy of the batch
+    # warm-up: W calls of the same loop (the first W budgets) on a separate copy of an eighth of the
+    # batch (module loading, table staging, clocks; the timed calls start from a fresh copy)
     if W > 0:
-        warm = HostLoop(km, args.form, d_tn, d_tt, tadv, d_state, caps[0], False, dev)
+        Bw = max(1, B // 8)
+        warm = HostLoop(km, args.form, d_tn, d_tt, tadv[:Bw], d_state[:Bw], caps[0], False, dev)
         for k in range(W):
             warm.advance(stream)
             warm.carry(stream, caps[k + 1] if k + 1 < K else UNCAPPED)
@@ -849,6 +856,9 @@ def engine_arm(args, world: int, rank: int, local: int):
                              "the FP32 side counts factorizations, solves and Jacobians"},
     }
 
+    if not args.no_e2e:
+        line["e2e"] = e2e_loop(km, state, tadv, tol_time, args.form, K, cap, world, dev, stream)
+
     if rank == 0:
         # plain FP64 form on a subsample (one uncapped call: its trajectory is that of the K calls, since
         # the plain form carries nothing between calls but t, dt and the state): its rate and the FP64
@@ -922,13 +932,15 @@ def engine_arm(args, world: int, rank: int, local: int):
             ("aerosol", args.aerosol_samples, lambda n: aerosol_leg(n, min(args.cpu_seconds, 5.0), dev, stream))]
     for key, n, fn in legs:
         if rank == 0 and n > 0:
+            if time.perf_counter() - T_START > args.leg_budget_s:
+                line[key] = {"skipped": f"the run passed {args.leg_budget_s:.0f} s before this leg started "
+                                        f"(--leg-budget-s); run it alone with its own option"}
+                continue
             t0 = time.perf_counter()
             line[key] = fn(n)
             line[key]["leg_wall_s"] = round(time.perf_counter() - t0, 1)
-
-    if not args.no_e2e:
-        line["e2e"] = e2e_loop(km, state, tadv, tol_time, args.form, K, cap, world, dev, stream)
     if rank == 0:
+        line["wall_s"] = round(time.perf_counter() - T_START, 1)
         print(json.dumps(line), flush=True)
 
 

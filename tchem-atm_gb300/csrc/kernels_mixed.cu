@@ -20,6 +20,8 @@ TCHEM_GB_DECLARE_SHAPE(mixed, 32, 1)
 TCHEM_GB_DECLARE_SHAPE(mixed, 52, 2)
 TCHEM_GB_DECLARE_SHAPE(mixed, 64, 2)
 TCHEM_GB_DECLARE_SHAPE(mixgj, 52, 1_g2)
+TCHEM_GB_DECLARE_SHAPE(mixgj, 64, 1_g2)
+TCHEM_GB_DECLARE_SHAPE(mixgj, 128, 1_g4)
 TCHEM_GB_DECLARE_SHAPE(simpl, 24, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 32, 1)
 TCHEM_GB_DECLARE_SHAPE(simpl, 52, 2)
@@ -54,6 +56,8 @@ const Variant* variants(int* n) {
       {52, 2, 1, 8, false, false, false, kernel_mixed_52_2(), &launch_mixed_52_2},
       {64, 2, 1, 8, false, false, false, kernel_mixed_64_2(), &launch_mixed_64_2},
       {52, 1, 2, 16, false, true, false, kernel_mixgj_52_1_g2(), &launch_mixgj_52_1_g2},
+      {64, 1, 2, 12, false, true, false, kernel_mixgj_64_1_g2(), &launch_mixgj_64_1_g2},
+      {128, 1, 4, 8, false, true, false, kernel_mixgj_128_1_g4(), &launch_mixgj_128_1_g4},
       {24, 1, 1, 12, true, true, false, kernel_simpl_24_1(), &launch_simpl_24_1},
       {32, 1, 1, 12, true, true, false, kernel_simpl_32_1(), &launch_simpl_32_1},
       {52, 2, 1, 8, true, true, false, kernel_simpl_52_2(), &launch_simpl_52_2},
@@ -93,7 +97,9 @@ MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_cou
   if (!best)
     throw std::domain_error(simplified ? "simplified form: no kernel shape for this mechanism size and threads_per_sample "
                                          "(up to 64 species with 32 or 64 threads, 128 with 128 threads)"
-                                       : "FP32-LU form: mechanisms with more than 64 active species are not supported");
+                                       : "full-Newton FP32 form: no kernel shape for this mechanism size and "
+                                         "threads_per_sample (LU up to 64 species with 32 threads; Gauss-Jordan "
+                                         "up to 64 species with 64 threads, 128 with 128 threads)");
   MixedLayout ml = mixed::make_layout(L, best->MC, best->gj, e3);
   ml.simplified = simplified ? 1 : (best->gj ? 2 : 0);
   const size_t gbytes = ml.warp_bytes;
