@@ -523,7 +523,7 @@ def aerosol_leg(B: int, cpu_seconds: float, dev, stream) -> dict:
     t = torch.zeros(B, dtype=torch.float64, device=dev)
     dt = torch.zeros_like(t)
     stats = torch.zeros(B * 8, dtype=torch.int32, device=dev)
-    ws = torch.empty(AerosolChemistry.getWorkSpaceSize(km, am, B), dtype=torch.uint8, device=dev)
+    ws = torch.zeros(AerosolChemistry.getWorkSpaceSize(km, am, B), dtype=torch.uint8, device=dev)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
 
     def run():
@@ -715,7 +715,8 @@ class HostLoop:
         self.status = torch.empty(B, dtype=torch.int32, device=dev)
         self.stats = torch.zeros(B, 8, dtype=torch.int32, device=dev) if stats else None
         self.total = torch.zeros(B, 8, dtype=torch.int64, device=dev) if stats else None
-        self.ws = torch.empty(AtmosphericChemistry.getWorkSpaceSize(km, B, form=form), dtype=torch.uint8, device=dev)
+        # zeroed: the device error word in the header persists until read, so it must start clear
+        self.ws = torch.zeros(AtmosphericChemistry.getWorkSpaceSize(km, B, form=form), dtype=torch.uint8, device=dev)
 
     def advance(self, stream):
         """One runDeviceBatch call (the time-advance kernel)."""

@@ -257,7 +257,10 @@ size_t tchem_gb_workspace_bytes(const tchem_gb_mech* const* mechs, int n_mechs, 
  *                      t_out >= tend are skipped, as the reference does) and written.
  *   status[nbatch]     tchem_gb_sample_status; stats[nbatch] optional work counters.
  *   workspace          device scratch of tchem_gb_workspace_bytes() bytes, or NULL to use a
- *                      library-owned cached allocation (not usable inside stream capture).
+ *                      library-owned cached allocation (not usable inside stream capture). A
+ *                      caller-owned workspace must be zero-filled before its first use: its header
+ *                      holds the device error word, which persists across calls until
+ *                      tchem_gb_device_error reads and clears it.
  * Stream-ordered and asynchronous. */
 int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const int32_t* mech_of_sample, int nbatch,
                           const double* tol_newton, const double* tol_time, const double* fac,

@@ -64,6 +64,13 @@ void* owned_workspace(int dev, size_t bytes) {
       cudaGetLastError();
       throw std::bad_alloc();
     }
+    // the header's device error word persists until tchem_gb_device_error reads it: start clear
+    if (cudaMemset(w.ptr, 0, kHeaderBytes) != cudaSuccess) {
+      cudaGetLastError();
+      cudaFree(w.ptr);
+      w.ptr = nullptr;
+      throw std::bad_alloc();
+    }
     w.bytes = want;
   }
   return w.ptr;

@@ -190,7 +190,7 @@ class AtmosphericChemistry:
         n = _capi.lib().tchem_gb_workspace_bytes(_handles(mechs), len(mechs), B, C.byref(o))
         if n == 0:
             _capi.check(1, "tchem_gb_workspace_bytes")
-        ws = torch.empty(int(n), dtype=torch.uint8, device=state.device)
+        ws = torch.zeros(int(n), dtype=torch.uint8, device=state.device)  # error word starts clear
         side = torch.cuda.Stream(device=state.device)
         side.wait_stream(torch.cuda.current_stream(state.device))
         with torch.cuda.stream(side):  # one eager run: mechanism tables on the device, kernel attributes set
