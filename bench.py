@@ -730,6 +730,16 @@ class HostLoop:
         self.AC.carry_over(self.tadv, self.t, self.dt, next_cap, stream=stream)
 
 
+def fma_probe() -> C.CDLL:
+    """The FMA-throughput probe library (built by tchem_gb.build beside the engine): FP64 and FP32
+    FLOP/s of this GPU, the roofline denominators that the measured GPU peaks do not list."""
+    from tchem_gb.build import PROBE_LIB_PATH
+    lib = C.CDLL(str(PROBE_LIB_PATH))
+    lib.tchem_gb_probe_fma_peak.restype = C.c_int
+    lib.tchem_gb_probe_fma_peak.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]
+    return lib
+
+
 def caps_for(K: int, cap: int) -> list[int]:
     """Step budgets of the K calls: `cap` for calls 1..K-1, none for the last."""
     return [cap] * (K - 1) + [UNCAPPED]
@@ -821,8 +831,9 @@ def engine_arm(args, world: int, rank: int, local: int):
     # roofline of the time-advance kernel: algorithmic flops over all K launches / their summed time
     f32, f64 = work_flops(km, stats)
     peak64, peak32 = C.c_double(), C.c_double()
-    L.tchem_gb_measure_fma_peak(1, 4, 4096, C.byref(peak64))
-    L.tchem_gb_measure_fma_peak(0, 4, 65536, C.byref(peak32))
+    probe = fma_probe()
+    _capi.check(probe.tchem_gb_probe_fma_peak(1, 4, 4096, C.byref(peak64)), "FP64 FMA probe")
+    _capi.check(probe.tchem_gb_probe_fma_peak(0, 4, 65536, C.byref(peak32)), "FP32 FMA probe")
     ach64 = f64 / (kernel_ms * 1e-3) / 1e12
     ach32 = f32 / (kernel_ms * 1e-3) / 1e12
     per_sample = NCU_DRAM_BYTES_PER_SAMPLE.get(args.form)
@@ -847,7 +858,7 @@ def engine_arm(args, world: int, rank: int, local: int):
         "roofline": {"bound": "fp64", "achieved": ach64, "peak": peak64.value / 1e12, "unit": "TFLOP/s",
                      "frac": ach64 / (peak64.value / 1e12), "traffic": traffic,
                      "kernel_ms": kernel_ms, "launches": K,
-                     "peak_source": "FMA-chain probe measured in this run (tchem_gb_measure_fma_peak); "
+                     "peak_source": "FMA-chain probe measured in this run (libtchem_gb_probe.so); "
                                     "MEASURED_PEAKS.json has no FP64/FP32 figure",
                      "traffic_source": "DRAM bytes per sample from one ncu capture of a 4096-sample case of this "
                                        "kernel, times the samples of one launch",

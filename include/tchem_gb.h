@@ -345,7 +345,9 @@ int tchem_gb_autotune(tchem_gb_mech* mech, int form, int nbatch, const double* t
 int tchem_gb_mech_set_threads_per_sample(tchem_gb_mech* mech, int form, int threads_per_sample);
 
 /* Synchronizes `stream`, then reads and clears the device error word of `workspace` (NULL: the
- * library-owned workspace). *device_error is 0 when no kernel reported a timed-out wait. */
+ * library-owned workspace). *device_error is 0 when no kernel reported a timed-out wait; bit 0
+ * (1): a bounded wait expired; bit 1 (2): a tensor-core kernel's MMAs had not completed when it
+ * released its tensor memory. */
 int tchem_gb_device_error(void* workspace, void* stream, int32_t* device_error);
 
 /* The carry-over step of the reference's host time loop between two tchem_gb_time_advance calls
@@ -460,11 +462,6 @@ int tchem_gb_tc_tile_update_tf32(int ntiles, int N, const float* A, const float*
  * has no usable pivot, -1 when a bounded wait expired. Device arrays; validation on a GPU is
  * pending. */
 int tchem_gb_tc_lu_factor_tf32(int nbatch, int m, int lda, float* A, int32_t* piv, int32_t* info, void* stream);
-
-/* Measurement helper (no counterpart in the reference): FMA throughput of the current device in
- * FLOP/s for FP64 (fp64 = 1) or FP32, from independent FMA chains on every SM. These are the
- * roofline denominators of the FP64-bound plain form and the FP32-bound mixed form. */
-int tchem_gb_measure_fma_peak(int fp64, int blocks_per_sm, int iters, double* flops_per_s);
 
 #ifdef __cplusplus
 }

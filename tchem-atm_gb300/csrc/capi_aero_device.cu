@@ -213,6 +213,7 @@ int tchem_gb_aero_time_advance(const tchem_gb_mech* mech, const tchem_gb_aero* a
                                double* t_out, double* dt_out, double* state_out, int32_t* status,
                                tchem_gb_sample_stats* stats, void* workspace, size_t workspace_bytes, void* stream_v) {
   (void)fac;
+  ProfileRegion region("TChem::AerosolChemistry::runDeviceBatch::kmcd array");
   const char* who = "tchem_gb_aero_time_advance";
   if (!mech || !aero || nbatch < 0) return fail(TCHEM_GB_ERR_ARG, std::string(who) + ": bad model or batch size");
   AeroDev A;

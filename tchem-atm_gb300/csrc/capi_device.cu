@@ -415,6 +415,8 @@ int tchem_gb_time_advance(const tchem_gb_mech* const* mechs, int n_mechs, const 
                           const tchem_gb_tadv* tadv, const double* state, double* t_out, double* dt_out,
                           double* state_out, int32_t* status, tchem_gb_sample_stats* stats, void* workspace,
                           size_t workspace_bytes, const tchem_gb_advance_opts* opts, void* stream_v) {
+  ProfileRegion region(mech_of_sample ? "TChem::AtmosphericChemistry::runDeviceBatch::kmcd array"
+                                      : "TChem::AtmosphericChemistry::runDeviceBatch::kmcd");
   return time_advance_impl(mechs, n_mechs, mech_of_sample, nbatch, tol_newton, tol_time, tadv, state, t_out, dt_out,
                            state_out, status, stats, workspace, workspace_bytes, opts, stream_v, TapeArgs{});
 }
@@ -727,6 +729,8 @@ int tchem_gb_time_advance_hostbuf(const tchem_gb_mech* const* mechs, int n_mechs
                                   const tchem_gb_tadv* tadv, const double* state, double* t_out,
                                   double* dt_out, double* state_out, int32_t* status, tchem_gb_sample_stats* stats,
                                   const tchem_gb_advance_opts* opts, void* stream_v) {
+  ProfileRegion region(mech_of_sample ? "TChem::AtmosphericChemistry::runHostBatch::kmcd array"
+                                      : "TChem::AtmosphericChemistry::runHostBatch::kmcd");
   if (!mechs || n_mechs <= 0 || nbatch < 0)
     return fail(TCHEM_GB_ERR_ARG, "tchem_gb_time_advance_hostbuf: bad mechanisms or batch size");
   if (nbatch == 0) return TCHEM_GB_OK;
@@ -910,6 +914,7 @@ int tchem_gb_e3sm_time_advance(const tchem_gb_mech* mech, int nbatch, const doub
                                const double* external_sources, double* t_out, double* dt_out, double* state_out,
                                int32_t* status, tchem_gb_sample_stats* stats, void* workspace,
                                size_t workspace_bytes, const tchem_gb_advance_opts* opts, void* stream_v) {
+  ProfileRegion region("TChem::AtmosphericChemistryE3SM::runDeviceBatch::kmcd");
   if (!mech || nbatch < 0 || n_photo < 0 || (n_photo > 0 && !photo_rates))
     return fail(TCHEM_GB_ERR_ARG, "tchem_gb_e3sm_time_advance: bad argument");
   if (nbatch == 0) return TCHEM_GB_OK;

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstddef>
 #include <string>
@@ -45,5 +46,16 @@ int workspace_bytes_checked(const tchem_gb_mech* const* mechs, int n_mechs, int 
 // Resolves the device address of tchem_gb_time_advance_noalloc's fixed scratch on device dev
 // (loading the module that holds it); returns false when the lookup failed.
 bool noalloc_setup(int dev);
+
+// A named profiling range around an entry point's host-side work (the launches it enqueues), under
+// the region names of the reference's Kokkos::Profiling::pushRegion calls (e.g.
+// src/core/TChem_AtmosphericChemistry.cpp:61,244), so NVTX-aware tools (nsys, ncu --nvtx) show the
+// same regions a kokkos-tools user sees. Header-only NVTX: no cost when no tool is attached.
+struct ProfileRegion {
+  explicit ProfileRegion(const char* name) { nvtxRangePushA(name); }
+  ~ProfileRegion() { nvtxRangePop(); }
+  ProfileRegion(const ProfileRegion&) = delete;
+  ProfileRegion& operator=(const ProfileRegion&) = delete;
+};
 
 }  // namespace tchem_gb

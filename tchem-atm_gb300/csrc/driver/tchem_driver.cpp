@@ -117,7 +117,9 @@ struct Driver {
                  "cudaMemcpy");
       bool done = true, advanced = false;
       for (size_t b = 0; b < B; ++b) {
-        if (status[b] == TCHEM_GB_SAMPLE_SKIPPED) continue;
+        // rows that failed in an earlier call are out of the step (their tend was set to their
+        // tbeg, so the kernel skips them) and do not count as progress
+        if (failed[b] || status[b] == TCHEM_GB_SAMPLE_SKIPPED) continue;
         if (status[b] == TCHEM_GB_SAMPLE_OK && t[b] > tadv[b].tbeg) advanced = true;
         total[b].n_steps += stats[b].n_steps;
         total[b].n_rejected += stats[b].n_rejected;
@@ -129,6 +131,7 @@ struct Driver {
         total[b].n_jac += stats[b].n_jac;
         if (status[b] != TCHEM_GB_SAMPLE_OK) {
           failed[b] = status[b];
+          tadv[b].tend = tadv[b].tbeg;  // no further work on this row in later calls
           continue;
         }
         tadv[b].tbeg = t[b];

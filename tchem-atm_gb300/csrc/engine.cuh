@@ -16,6 +16,9 @@ constexpr int kMaxGroupMechs = 8;
 // kErrBarrierTimeout in its error word and returns.
 constexpr long long kSpinLimit = 1ll << 24;
 constexpr int kErrBarrierTimeout = 1;
+// A tensor-core kernel's second bounded wait for its MMAs also expired: it freed its TMEM while
+// MMAs may still have been writing it (set together with kErrBarrierTimeout).
+constexpr int kErrMmaInFlight = 2;
 
 // Shared-memory views of the staged tables.
 struct SmemTables {

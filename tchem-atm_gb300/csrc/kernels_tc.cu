@@ -74,7 +74,10 @@ __global__ void __launch_bounds__(128, 1) tc_tile_update_kernel(int N, uint32_t 
   ok = __syncthreads_and(ok ? 1 : 0) != 0;
   if (!ok) {
     if (tid == 0) atomicOr(error_word, kErrBarrierTimeout);
-    tc::mbar_wait(mbar, 0, kSpinLimit);  // a second bounded window for the MMAs in flight
+    // a second bounded window for the MMAs in flight; if it also expires, the TMEM below is freed
+    // while MMAs may still write it, which the error word records
+    const bool drained = __syncthreads_and(tc::mbar_wait(mbar, 0, kSpinLimit) ? 1 : 0) != 0;
+    if (!drained && tid == 0) atomicOr(error_word, kErrMmaInFlight);
   }
   tc::fence_after_sync();
   if (ok) {
@@ -232,7 +235,10 @@ __global__ void __launch_bounds__(128, 1) tc_lu_kernel(int m, int lda, float* A,
         done = __syncthreads_and(done ? 1 : 0) != 0;
         if (!done) {
           if (tid == 0) atomicOr(error_word, kErrBarrierTimeout);
-          tc::mbar_wait(mbar, ph, kSpinLimit);  // a second bounded window for the MMAs in flight
+          // a second bounded window for the MMAs in flight (expired too: TMEM is freed while MMAs
+          // may still write it, recorded in the error word)
+          const bool drained = __syncthreads_and(tc::mbar_wait(mbar, ph, kSpinLimit) ? 1 : 0) != 0;
+          if (!drained && tid == 0) atomicOr(error_word, kErrMmaInFlight);
           status = -1;
         }
         tc::fence_after_sync();

@@ -1,13 +1,14 @@
-// FMA-throughput probe: the roofline denominators of the time-advance kernels.
+// FMA-throughput probe of the benchmark (libtchem_gb_probe.so, not part of the engine library):
+// the roofline denominators of the time-advance kernels.
 //
 // The time advance is bound by arithmetic, not memory: the plain form by the FP64 pipe, the
-// mixed form by FP32 FMA. The probe runs 8 independent FMA chains per thread on a grid that
-// fills every SM and reports FLOP/s (2 per FMA).
+// mixed form by FP32 FMA, and the measured GPU peaks list only HBM and BF16 tensor figures. The
+// probe runs 8 independent FMA chains per thread on a grid that fills every SM and reports
+// FLOP/s (2 per FMA). Return codes: 0 ok, 1 bad argument, 3 CUDA error, 5 allocation failed.
 #include <cuda_runtime.h>
 
 #include <cstdint>
 
-#include "../../include/tchem_gb.h"
 
 namespace {
 
@@ -33,7 +34,7 @@ int measure(int blocks_per_sm, int iters, double* flops_per_s) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   const int grid = sms * blocks_per_sm, block = 256;
   T* out = nullptr;
-  if (cudaMalloc(&out, sizeof(T) * grid * block) != cudaSuccess) return TCHEM_GB_ERR_NOMEM;
+  if (cudaMalloc(&out, sizeof(T) * grid * block) != cudaSuccess) return 5;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -47,15 +48,15 @@ int measure(int blocks_per_sm, int iters, double* flops_per_s) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   cudaFree(out);
-  if (e != cudaSuccess) return TCHEM_GB_ERR_CUDA;
+  if (e != cudaSuccess) return 3;
   const double flops = 2.0 * 8.0 * 16.0 * static_cast<double>(iters) * grid * block;
   *flops_per_s = flops / (ms * 1e-3);
-  return TCHEM_GB_OK;
+  return 0;
 }
 
 }  // namespace
 
-extern "C" int tchem_gb_measure_fma_peak(int fp64, int blocks_per_sm, int iters, double* flops_per_s) {
-  if (!flops_per_s || blocks_per_sm <= 0 || iters <= 0) return TCHEM_GB_ERR_ARG;
+extern "C" int tchem_gb_probe_fma_peak(int fp64, int blocks_per_sm, int iters, double* flops_per_s) {
+  if (!flops_per_s || blocks_per_sm <= 0 || iters <= 0) return 1;
   return fp64 ? measure<double>(blocks_per_sm, iters, flops_per_s) : measure<float>(blocks_per_sm, iters, flops_per_s);
 }

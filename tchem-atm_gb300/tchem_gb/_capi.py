@@ -128,7 +128,6 @@ def lib() -> C.CDLL:
         "tchem_gb_kforward": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp]),
         "tchem_gb_reaction_rates": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp]),
         "tchem_gb_jacobian": (C.c_int, [C.POINTER(vp), C.c_int, vp, C.c_int, vp, vp, vp]),
-        "tchem_gb_measure_fma_peak": (C.c_int, [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_double)]),
         "tchem_gb_time_advance_record": (C.c_int, [vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                                    C.c_int, vp]),
         "tchem_gb_adjoint_workspace_bytes": (C.c_size_t, [vp, C.c_int]),

@@ -1,6 +1,7 @@
 """Builds libtchem_gb.so (the engine: sm_103a CUDA kernels + C ABI) in-tree, and beside it
 libtchem_gb_driver.so (the host-model driver interface of include/tchem_gb_driver.h, host code
-over libtchem_gb.so).
+over libtchem_gb.so) and libtchem_gb_probe.so (the benchmark's FMA-throughput probe, kept out of
+the engine library).
 
 Translation units are compiled in parallel with nvcc and linked into
 ``tchem-atm_gb300/tchem_gb/libtchem_gb.so``. Nothing here depends on torch.
@@ -18,6 +19,8 @@ PKG_DIR = Path(__file__).resolve().parent
 SRC_DIR = PKG_DIR.parent / "csrc"
 BUILD_DIR = PKG_DIR.parent / "_build"
 LIB_PATH = PKG_DIR / "libtchem_gb.so"
+PROBE_LIB_PATH = PKG_DIR / "libtchem_gb_probe.so"  # the benchmark's FMA-peak probe, not the engine
+PROBE_SRC = SRC_DIR / "probe" / "fma_peak.cu"
 DRIVER_LIB_PATH = PKG_DIR / "libtchem_gb_driver.so"
 DRIVER_DIR = SRC_DIR / "driver"
 
@@ -54,15 +57,21 @@ def build(verbose: bool = False, extra_flags: list[str] | None = None, force: bo
     srcs = sources()
     extra = list(extra_flags or [])
     driver_srcs = sorted(DRIVER_DIR.glob("*.cpp"))
-    if not force and LIB_PATH.exists() and DRIVER_LIB_PATH.exists():
-        deps = srcs + driver_srcs + list(SRC_DIR.glob("*.h*")) + list(SRC_DIR.glob("*.cuh"))
+    outs = (LIB_PATH, DRIVER_LIB_PATH, PROBE_LIB_PATH)
+    if not force and all(p.exists() for p in outs):
+        deps = srcs + driver_srcs + [PROBE_SRC] + list(SRC_DIR.glob("*.h*")) + list(SRC_DIR.glob("*.cuh"))
         deps += [h for h in (PKG_DIR.parent.parent / "include").glob("tchem_gb*.h")]
         newest = max(p.stat().st_mtime for p in deps)
-        if min(LIB_PATH.stat().st_mtime, DRIVER_LIB_PATH.stat().st_mtime) > newest and not extra:
+        if min(p.stat().st_mtime for p in outs) > newest and not extra:
             return LIB_PATH
     workers = min(len(srcs), os.cpu_count() or 4)
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
-        objs = list(ex.map(lambda s: _compile(nvcc, s, extra), srcs))
+        objs = list(ex.map(lambda s: _compile(nvcc, s, extra), srcs + [PROBE_SRC]))
+    probe_obj = objs.pop()
+    cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(PROBE_LIB_PATH), str(probe_obj), "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
     cmd = [nvcc, *ARCH_FLAGS, "-shared", "-o", str(LIB_PATH), *map(str, objs), "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
