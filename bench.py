@@ -68,7 +68,7 @@ FORM_DTYPE = {"plain": "f64", "mixed": "f64 state / f32 Gauss-Jordan inverse or 
 # the same kernel (dram__bytes_read.sum + dram__bytes_write.sum over the launch, divided by the
 # samples). The per-sample traffic (state, time-advance record and times read once, results written
 # once) does not depend on the horizon or on the batch size, so it scales by samples.
-NCU_DRAM_BYTES_PER_SAMPLE: dict[str, float] = {}
+NCU_DRAM_BYTES_PER_SAMPLE = {"mixed": 820480 / 1216}  # 1,216-sample capture of the two-warp Gauss-Jordan kernel
 
 
 def parse() -> argparse.Namespace:
@@ -837,7 +837,7 @@ def engine_arm(args, world: int, rank: int, local: int):
     ach64 = f64 / (kernel_ms * 1e-3) / 1e12
     ach32 = f32 / (kernel_ms * 1e-3) / 1e12
     per_sample = NCU_DRAM_BYTES_PER_SAMPLE.get(args.form)
-    traffic = None if per_sample is None else per_sample * B / K
+    traffic = None if per_sample is None else per_sample * B  # every launch reads each sample's row
 
     line = {
         "metric": METRIC, "value": value, "unit": "samples/s", "n_gpus": world, "steps": K,

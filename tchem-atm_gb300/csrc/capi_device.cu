@@ -117,6 +117,7 @@ struct GroupPlan {
   size_t gmat_offset = 0;
   size_t gmat_elems_per_warp = 0;
   int threads_per_sample = 32;
+  bool tc = false;  // the tensor-core form (kernels_tc_advance.cu)
   MixedLayout ml{};
 };
 
@@ -178,6 +179,29 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
     const MechLayout& L = g.dev.L;
     plan.m_max = std::max(plan.m_max, L.m);
     g.form = o.form;
+    if (mixed && L.m > 128 && !e3sm) {
+      // beyond the register-resident shapes: the tensor-core full-Newton form, one sample per CTA
+      if (L.m > tc_advance_max_species())
+        throw std::domain_error("mixed forms: mechanisms with more than " + std::to_string(tc_advance_max_species()) +
+                                " active species run in the plain form only");
+      if (o.threads_per_sample != 0 && o.threads_per_sample != 128)
+        throw std::domain_error("tensor-core form (more than 128 species): threads_per_sample must be 0 or 128");
+      g.tc = true;
+      g.dev = dts[g.mechs[0]]->dev;  // CSR tables, read from global memory
+      g.form = o.form;
+      g.threads_per_sample = 128;
+      g.warps_per_block = 4;
+      g.smem = tc_advance_smem_bytes(L);
+      if (g.smem > static_cast<size_t>(info.max_smem_optin))
+        throw std::domain_error("tensor-core form: working set larger than shared memory");
+      g.grid = std::max(1, std::min(info.sm_count, std::max(nbatch, 1)));
+      g.matrix_in_smem = false;
+      g.lda = 0;
+      g.gmat_elems_per_warp = tc_advance_matrix_floats();  // floats per CTA
+      g.gmat_offset = off;
+      off += up256(sizeof(float) * g.gmat_elems_per_warp * static_cast<size_t>(g.grid));
+      continue;
+    }
     if (mixed) {
       int tps = o.threads_per_sample;
       if (tps == 0 && o.form >= 0 && o.form < 3) tps = mechs[g.mechs[0]]->tps_pref[o.form];
@@ -395,7 +419,9 @@ int time_advance_impl(const tchem_gb_mech* const* mechs, int n_mechs, const int3
     P.keff_in = rates.keff;
     P.src_in = rates.src;
     P.src_stride = rates.src_stride;
-    if (gp.form == TCHEM_GB_FORM_MIXED || gp.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED)
+    if (gp.tc)
+      e = launch_trbdf2_tc(P, gp.grid, gp.smem, stream);
+    else if (gp.form == TCHEM_GB_FORM_MIXED || gp.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED)
       e = launch_trbdf2_mixed(P, gp.dev.L, gp.grid, gp.warps_per_block, gp.smem, gp.threads_per_sample, stream);
     else
       e = launch_trbdf2_fp64(P, gp.grid, gp.warps_per_block, gp.smem, stream);

@@ -13,6 +13,15 @@ cudaError_t launch_trbdf2_fp64(const AdvanceParams& P, int grid, int warps_per_b
                                cudaStream_t stream);
 const void* trbdf2_fp64_kernel_ptr(int m);
 
+// Tensor-core full-Newton form for mechanisms of 129 to tc_advance_max_species() active species
+// (kernels_tc_advance.cu): one CTA of 128 threads per sample, one CTA per SM, the FP32 Newton
+// matrix in a global slot of tc_advance_matrix_floats() floats per CTA (AdvanceParams::gmat,
+// gmat_stride in floats).
+size_t tc_advance_smem_bytes(const MechLayout& L);
+size_t tc_advance_matrix_floats();
+int tc_advance_max_species();
+cudaError_t launch_trbdf2_tc(const AdvanceParams& P, int grid, size_t smem, cudaStream_t stream);
+
 // Discrete adjoint of the plain form (kernels_adjoint.cu): one warp per sample, one mechanism.
 struct AdjointParams {
   MechDev mech;
