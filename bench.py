@@ -94,13 +94,14 @@ def parse() -> argparse.Namespace:
                     help="samples of the discrete-adjoint leg (1800 s horizon, FP64); 0 skips it")
     ap.add_argument("--e3sm-samples", type=int, default=65536,
                     help="samples of the E3SM leg (the reference's 80-column uci scenario tiled); 0 skips it")
-    ap.add_argument("--large-samples", type=int, default=0,
-                    help="samples of the 300-species / 1000-reaction leg in the plain FP64 form (the baseline the "
-                         "tensor-core factorization is compared with), 10 s horizon; 0 skips it")
+    ap.add_argument("--large-samples", type=int, default=1216,
+                    help="samples of the 300-species / 1000-reaction leg in the tensor-core form (with the plain "
+                         "FP64 form beside it on 152 samples over 0.1 s); 0 skips it")
+    ap.add_argument("--large-horizon", type=float, default=10.0, help="horizon of the 300-species leg (s)")
     ap.add_argument("--tc-lu-matrices", type=int, default=0,
                     help="matrices of the tensor-core LU leg (300 x 300 FP32, TF32 trailing updates on tcgen05): "
                          "factorizations/s and the TF32 rate of the trailing updates; 0 skips it")
-    ap.add_argument("--leg-budget-s", type=float, default=1000.0,
+    ap.add_argument("--leg-budget-s", type=float, default=1150.0,
                     help="side legs start only while the run's wall time is below this (seconds)")
     ap.add_argument("--aerosol-samples", type=int, default=8192,
                     help="samples of the gas-aerosol (SIMPOL.1) leg: the reference driver test's CB05CL_AE5 + SOA "
@@ -344,7 +345,6 @@ def uneven_leg(B: int, form: str, dev, stream) -> dict:
     dt = torch.zeros_like(t)
     g, status = AtmosphericChemistry.capture(d_tn, d_tt, tadv_to_device(tadv, dev), d_state, t, dt, out, mechs,
                                              mech_of_sample=torch.as_tensor(mos).to(dev), form=form)
-    g.replay()  # warm-up replay (the capture helper also ran the batch once eagerly)
     torch.cuda.synchronize(dev)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
@@ -353,10 +353,10 @@ def uneven_leg(B: int, form: str, dev, stream) -> dict:
     torch.cuda.synchronize(dev)
     ms = e0.elapsed_time(e1)
     res = out.cpu().numpy()
-    # accuracy: 512 samples of each 51-species variant and 64 of each 120-species variant against the
-    # plain FP64 form (one call per mechanism)
+    # accuracy: 512 samples of each 51-species variant and 16 of each 120-species variant against the
+    # plain FP64 form (one call per mechanism; the plain form is slow at 120 species)
     acc = {}
-    for k, n in ((0, 512), (1, 512), (2, 64), (3, 64)):
+    for k, n in ((0, 512), (1, 512), (2, 16), (3, 16)):
         sel = np.nonzero(mos == k)[0][:n]
         km = mechs[k]
         st = torch.as_tensor(state[sel][:, :km.state_dim]).to(dev)
@@ -372,7 +372,8 @@ def uneven_leg(B: int, form: str, dev, stream) -> dict:
     return {"samples": B, "value": B / (ms * 1e-3), "unit": "samples/s", "ms": ms, "form": form,
             "failed_samples": int((status.cpu().numpy() != 0).sum()),
             "mix": {"51_species": int((~big).sum()), "120_species": int(big.sum()), "night": int(night.sum())},
-            "launch": "one CUDA graph (t reset, bucketing, one persistent kernel per mechanism structure)",
+            "launch": "one CUDA graph replay, timed (t reset, bucketing, one persistent kernel per mechanism "
+                      "structure, the structures' kernels concurrent on forked streams)",
             "autotuned": tuned, "accuracy_vs_plain_fp64_gpu": acc}
 
 
@@ -570,42 +571,60 @@ def aerosol_leg(B: int, cpu_seconds: float, dev, stream) -> dict:
                                        f"over samples on {cores} threads ({el:.2f} s)"}}
 
 
-# ---- 300-species mechanism, plain FP64 ---------------------------------------------------------
+# ---- 300-species mechanism: the tensor-core form ------------------------------------------------
 
-def large_leg(B: int, dev, stream) -> dict:
+LARGE_SPEC = dict(n_species=300, n_reactions=1000, seed=20251205)
+
+
+def large_leg(B: int, horizon: float, dev, stream) -> dict:
     """The seeded 300-species / 1000-reaction mechanism (the large dense-LU configuration: same rate
-    mix, at most 2 reactants and 4 products) in the plain FP64 form, B samples over 10 s (a short
-    horizon of the 3600 s configuration, which the plain form would take hours to cover at this
-    size); the first 2 end states against the FP64 oracle."""
+    mix, at most 2 reactants and 4 products) in the tensor-core form (full Newton; FP32 Newton
+    matrix, blocked LU with TF32 tcgen05 trailing updates, FP64 refinement), B samples over
+    `horizon`; the first 4 end states against the FP64 oracle; and the plain FP64 form beside it on
+    152 samples (one sample per SM) over 0.1 s, with the tensor-core form on the same 152 samples and
+    horizon, for the rate ratio."""
     import torch
     from oracle import Oracle
     from tchem_gb import AtmosphericChemistry, tadv_to_device, time_advance_array
-    km = KineticModel.from_string(mechanism_yaml(MechanismSpec(n_species=300, n_reactions=1000, seed=20251205)))
+    km = KineticModel.from_string(mechanism_yaml(MechanismSpec(**LARGE_SPEC)))
     m = km.n_active
     state = sample_states(B, m, seed=SEED + 21)
-    tadv = time_advance_array(B, tend=10.0, dt=1e-10, dtmin=1e-10, dtmax=10.0, max_num_newton_iterations=20,
-                              num_time_iterations_per_interval=10**7)
     tol_time = np.tile([ATOL, RTOL], (m, 1))
     d = lambda a: torch.as_tensor(np.ascontiguousarray(a)).to(dev)  # noqa: E731
-    d_state, d_tadv, d_tt = d(state), tadv_to_device(tadv, dev), d(tol_time)
-    d_tn = torch.tensor(TOL_NEWTON, dtype=torch.float64, device=dev)
-    out = torch.empty_like(d_state)
-    t = torch.zeros(B, dtype=torch.float64, device=dev)
-    dt = torch.zeros_like(t)
+    d_tn, d_tt = torch.tensor(TOL_NEWTON, dtype=torch.float64, device=dev), d(tol_time)
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-    ev[0].record(stream)
-    status = AtmosphericChemistry.runDeviceBatch(d_tn, d_tt, None, d_tadv, d_state, t, dt, out, km, form="plain",
-                                                 stream=stream)
-    ev[1].record(stream)
-    torch.cuda.synchronize(dev)
-    ms = ev[0].elapsed_time(ev[1])
-    K = min(2, B)
+
+    def run(form, n, hz):
+        tadv = time_advance_array(n, tend=hz, dt=1e-10, dtmin=1e-10, dtmax=hz, max_num_newton_iterations=20,
+                                  num_time_iterations_per_interval=10**7)
+        d_state = d(state[:n])
+        out = torch.empty_like(d_state)
+        t = torch.zeros(n, dtype=torch.float64, device=dev)
+        dt = torch.zeros_like(t)
+        stats = torch.zeros(n, 8, dtype=torch.int32, device=dev)
+        ev[0].record(stream)
+        st = AtmosphericChemistry.runDeviceBatch(d_tn, d_tt, None, tadv_to_device(tadv, dev), d_state, t, dt, out, km,
+                                                 stats=stats, form=form, stream=stream)
+        ev[1].record(stream)
+        torch.cuda.synchronize(dev)
+        return (ev[0].elapsed_time(ev[1]), out.cpu().numpy(), int((st != 0).sum().item()),
+                stats.cpu().numpy().astype(np.float64).mean(axis=0), tadv)
+
+    run("mixed", min(B, 152), 1e-3)  # warm-up: module load, kernel attributes, workspace
+    ms, res, bad, work, tadv = run("mixed", B, horizon)
+    K = min(4, B)
     ref = Oracle([km], native=True).time_advance(tadv[:K], state[:K], TOL_NEWTON, tol_time)[0]
-    res = out[:K].cpu().numpy()
-    err = rel_err(res[:, 3:3 + m], ref[:, 3:3 + m])
-    return {"samples": B, "species": m, "reactions": km.nReac, "horizon_s": 10.0, "form": "plain", "ms": ms,
-            "value": B / (ms * 1e-3), "unit": "samples/s", "status_ok": int((status == 0).sum().item()),
-            "max_rel_err_vs_oracle": float(err.max())}
+    err = rel_err(res[:K, 3:3 + m], ref[:, 3:3 + m])
+    P = min(152, B)
+    ms_tc, *_ = run("mixed", P, 0.1)
+    ms_pl, res_pl, bad_pl, *_ = run("plain", P, 0.1)
+    names = ["steps", "rejected", "newton_fail", "newton_iter", "factorizations", "solves", "rhs", "jacobians"]
+    return {"samples": B, "species": m, "reactions": km.nReac, "horizon_s": horizon, "form": "tensor-core full Newton",
+            "ms": ms, "value": B / (ms * 1e-3), "unit": "samples/s", "failed_samples": bad,
+            "work_per_sample": {k: float(v) for k, v in zip(names, work)},
+            "accuracy_vs_fp64_oracle": {"samples": K, "max": float(err.max()), "bound": 1e-6},
+            "vs_plain_fp64": {"samples": P, "horizon_s": 0.1, "tensor_core_ms": ms_tc, "plain_fp64_ms": ms_pl,
+                              "speedup": ms_pl / ms_tc, "plain_failed_samples": bad_pl}}
 
 
 # ---- tensor-core LU (300-species factorization) -----------------------------------------------
@@ -936,12 +955,12 @@ def engine_arm(args, world: int, rank: int, local: int):
             line["plain_fp64"]["accuracy_vs_fp64_oracle"] = {"samples": min(n, P), "max": float(eo.max()),
                                                              "bound": 1e-8}
 
-    legs = [("uneven_batch", args.uneven_samples, lambda n: uneven_leg(n, args.form, dev, stream)),
+    legs = [("e3sm", args.e3sm_samples, lambda n: e3sm_leg(n, min(args.cpu_seconds, 5.0), dev, stream)),
+            ("large_mechanism", args.large_samples, lambda n: large_leg(n, args.large_horizon, dev, stream)),
+            ("uneven_batch", args.uneven_samples, lambda n: uneven_leg(n, args.form, dev, stream)),
             ("adjoint", args.adjoint_samples, lambda n: adjoint_leg(km, state, tol_time, n, dev, stream)),
-            ("e3sm", args.e3sm_samples, lambda n: e3sm_leg(n, min(args.cpu_seconds, 5.0), dev, stream)),
-            ("large_mechanism", args.large_samples, lambda n: large_leg(n, dev, stream)),
-            ("tc_lu", args.tc_lu_matrices, lambda n: tc_lu_leg(n, dev, stream)),
-            ("aerosol", args.aerosol_samples, lambda n: aerosol_leg(n, min(args.cpu_seconds, 5.0), dev, stream))]
+            ("aerosol", args.aerosol_samples, lambda n: aerosol_leg(n, min(args.cpu_seconds, 5.0), dev, stream)),
+            ("tc_lu", args.tc_lu_matrices, lambda n: tc_lu_leg(n, dev, stream))]
     for key, n, fn in legs:
         if rank == 0 and n > 0:
             if time.perf_counter() - T_START > args.leg_budget_s:

@@ -4,6 +4,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <stdexcept>
 #include <string>
@@ -80,6 +81,39 @@ void* owned_workspace_peek(int dev) {
   std::lock_guard<std::mutex> lk(g_ws_mu);
   return static_cast<int>(g_ws.size()) > dev ? g_ws[dev].ptr : nullptr;
 }
+
+namespace {
+// Library-owned side streams and events per device: the kernels of a batch's mechanism-structure
+// groups run concurrently, forked from and joined back into the caller's stream.
+constexpr int kSideStreams = 15;  // groups beyond the first (kMaxGroups - 1)
+struct SideStreams {
+  cudaStream_t s[kSideStreams] = {};
+  cudaEvent_t fork = nullptr, join[kSideStreams] = {};
+  bool ready = false;
+  std::mutex mu;  // held from the fork to the join of one call
+};
+std::mutex g_side_mu;
+std::vector<std::unique_ptr<SideStreams>> g_side;
+
+// The device's side streams (created on first use); nullptr when creation failed.
+SideStreams* side_streams(int dev) {
+  std::lock_guard<std::mutex> lk(g_side_mu);
+  while (static_cast<int>(g_side.size()) <= dev) g_side.emplace_back(new SideStreams());
+  SideStreams& ss = *g_side[dev];
+  if (!ss.ready) {
+    bool ok = cudaEventCreateWithFlags(&ss.fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < kSideStreams && ok; ++i)
+      ok = cudaStreamCreateWithFlags(&ss.s[i], cudaStreamNonBlocking) == cudaSuccess &&
+           cudaEventCreateWithFlags(&ss.join[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    ss.ready = true;
+  }
+  return &ss;
+}
+}  // namespace
 
 int fail(int code, const std::string& msg) {
   set_last_error(msg);
@@ -380,8 +414,32 @@ int time_advance_impl(const tchem_gb_mech* const* mechs, int n_mechs, const int3
     if (e != cudaSuccess) return cuda_fail(e, "bucket kernel");
     note_launch();
   }
-  for (size_t g = 0; g < plan.groups.size(); ++g) {
+  // Groups of different mechanism structures run concurrently: the largest mechanism's kernel is
+  // launched first on the caller's stream, the others on side streams forked from it, so the
+  // SMs that the first kernel's persistent CTAs release as its queue drains take the next
+  // kernel's CTAs (no idle tail between kernels); the caller's stream joins them all.
+  std::vector<size_t> order(plan.groups.size());
+  for (size_t g = 0; g < order.size(); ++g) order[g] = g;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](size_t a, size_t b) { return plan.groups[a].dev.L.m > plan.groups[b].dev.L.m; });
+  SideStreams* side = nullptr;
+  std::unique_lock<std::mutex> side_lock;  // one caller at a time enqueues on the shared side streams
+  if (plan.groups.size() > 1) {
+    side = side_streams(dev);
+    if (!side) return fail(TCHEM_GB_ERR_CUDA, "tchem_gb_time_advance: side stream creation failed");
+    side_lock = std::unique_lock<std::mutex>(side->mu);
+    e = cudaEventRecord(side->fork, stream);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaEventRecord(fork)");
+  }
+  for (size_t oi = 0; oi < order.size(); ++oi) {
+    const size_t g = order[oi];
     const GroupPlan& gp = plan.groups[g];
+    cudaStream_t gs = stream;
+    if (oi > 0) {
+      gs = side->s[oi - 1];
+      e = cudaStreamWaitEvent(gs, side->fork, 0);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaStreamWaitEvent(fork)");
+    }
     AdvanceParams P{};
     P.mech = gp.dev;
     fill_slots(gp, mechs, dev, n_mechs, P.rate_param, P.slot_of_mech);
@@ -420,13 +478,18 @@ int time_advance_impl(const tchem_gb_mech* const* mechs, int n_mechs, const int3
     P.src_in = rates.src;
     P.src_stride = rates.src_stride;
     if (gp.tc)
-      e = launch_trbdf2_tc(P, gp.grid, gp.smem, stream);
+      e = launch_trbdf2_tc(P, gp.grid, gp.smem, gs);
     else if (gp.form == TCHEM_GB_FORM_MIXED || gp.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED)
-      e = launch_trbdf2_mixed(P, gp.dev.L, gp.grid, gp.warps_per_block, gp.smem, gp.threads_per_sample, stream);
+      e = launch_trbdf2_mixed(P, gp.dev.L, gp.grid, gp.warps_per_block, gp.smem, gp.threads_per_sample, gs);
     else
-      e = launch_trbdf2_fp64(P, gp.grid, gp.warps_per_block, gp.smem, stream);
+      e = launch_trbdf2_fp64(P, gp.grid, gp.warps_per_block, gp.smem, gs);
     if (e != cudaSuccess) return cuda_fail(e, "time-advance kernel launch");
     note_launch();
+    if (oi > 0) {
+      e = cudaEventRecord(side->join[oi - 1], gs);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(stream, side->join[oi - 1], 0);
+      if (e != cudaSuccess) return cuda_fail(e, "stream join");
+    }
   }
   return TCHEM_GB_OK;
 }

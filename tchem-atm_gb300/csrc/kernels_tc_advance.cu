@@ -265,23 +265,38 @@ struct Solver {
   __device__ void drain_tile(int b, int rt, int p1, int n0, int N) {
     const int lr = p1 + 128 * rt + tid;  // logical row
     float* row = lr < m ? A + static_cast<size_t>(perm[lr]) * kLda : nullptr;
-    for (int c = 0; c < N; c += 16) {
-      float pv[16];
-      tc::tmem_ld16(tmem + static_cast<uint32_t>(b) * 256u, warp, c, pv);  // warp-uniform
-      const int col = p1 + n0 + c;
-      if (row == nullptr || col >= m) continue;
-      if (col + 16 <= m) {
+    // 64 columns at a time: the row segment's global loads are all issued before the TMEM reads
+    for (int c0 = 0; c0 < N; c0 += 64) {
+      const int base = p1 + n0 + c0;
+      float4 g[16];
 #pragma unroll
-        for (int g = 0; g < 4; ++g) {
-          float4 a = *reinterpret_cast<float4*>(row + col + 4 * g);
-          a.x -= pv[4 * g];
-          a.y -= pv[4 * g + 1];
-          a.z -= pv[4 * g + 2];
-          a.w -= pv[4 * g + 3];
-          *reinterpret_cast<float4*>(row + col + 4 * g) = a;
+      for (int q = 0; q < 16; ++q) {
+        const int col = base + 4 * q;
+        g[q] = (row != nullptr && 4 * q < N - c0 && col + 4 <= m) ? *reinterpret_cast<const float4*>(row + col)
+                                                                  : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+#pragma unroll
+      for (int sc = 0; sc < 4; ++sc) {
+        if (16 * sc < N - c0) {  // warp-uniform
+          float pv[16];
+          tc::tmem_ld16(tmem + static_cast<uint32_t>(b) * 256u, warp, c0 + 16 * sc, pv);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            float4& a = g[4 * sc + q];
+            a.x -= pv[4 * q];
+            a.y -= pv[4 * q + 1];
+            a.z -= pv[4 * q + 2];
+            a.w -= pv[4 * q + 3];
+            const int col = base + 16 * sc + 4 * q;
+            if (row == nullptr || col >= m) continue;
+            if (col + 4 <= m) {
+              *reinterpret_cast<float4*>(row + col) = a;
+            } else {  // the ragged end of the row
+              const float* pq = pv + 4 * q;
+              for (int z = 0; col + z < m; ++z) row[col + z] -= pq[z];
+            }
+          }
         }
-      } else {
-        for (int qq = 0; qq < 16 && col + qq < m; ++qq) row[col + qq] -= pv[qq];
       }
     }
   }
@@ -291,10 +306,17 @@ struct Solver {
   __device__ bool lu_factor() {
     for (int k0 = 0; k0 < m; k0 += kPW) {
       const int kb = min(kPW, m - k0), p1 = k0 + kb, np = m - k0;
-      // panel rows k0 .. m-1 (logical), columns k0 .. k0 + 31, into shared memory
-      for (int e = tid; e < np * kPW; e += kNT) {
-        const int r = e / kPW, c = e - r * kPW;
-        pn[r * kPLd + c] = c < kb ? A[static_cast<size_t>(perm[k0 + r]) * kLda + k0 + c] : 0.f;
+      // panel rows k0 .. m-1 (logical), columns k0 .. k0 + 31, into shared memory: 8 float4 per row
+      // (k0 is a multiple of 32 and kLda of 4, so the loads are 16-byte aligned and stay inside the row)
+#pragma unroll 4
+      for (int e = tid; e < np * 8; e += kNT) {
+        const int r = e >> 3, c = 4 * (e & 7);
+        const float4 a = *reinterpret_cast<const float4*>(A + static_cast<size_t>(perm[k0 + r]) * kLda + k0 + c);
+        float* d = pn + r * kPLd + c;
+        d[0] = c < kb ? a.x : 0.f;
+        d[1] = c + 1 < kb ? a.y : 0.f;
+        d[2] = c + 2 < kb ? a.z : 0.f;
+        d[3] = c + 3 < kb ? a.w : 0.f;
       }
       __syncthreads();
       for (int c = 0; c < kb; ++c) {
@@ -355,10 +377,17 @@ struct Solver {
         }
         __syncthreads();
       }
-      // the factored panel back to the matrix (physical rows)
-      for (int e = tid; e < np * kPW; e += kNT) {
-        const int r = e / kPW, c = e - r * kPW;
-        if (c < kb) A[static_cast<size_t>(perm[k0 + r]) * kLda + k0 + c] = pn[r * kPLd + c];
+      // the factored panel back to the matrix (physical rows), 8 float4 per row
+#pragma unroll 4
+      for (int e = tid; e < np * 8; e += kNT) {
+        const int r = e >> 3, c = 4 * (e & 7);
+        float* dst = A + static_cast<size_t>(perm[k0 + r]) * kLda + k0 + c;
+        const float* src = pn + r * kPLd + c;
+        if (c + 4 <= kb) {
+          *reinterpret_cast<float4*>(dst) = make_float4(src[0], src[1], src[2], src[3]);
+        } else {
+          for (int z = 0; c + z < kb; ++z) dst[z] = src[z];
+        }
       }
       const int W = m - p1;  // trailing width
       if (W <= 0) break;
@@ -424,6 +453,26 @@ struct Solver {
     return true;
   }
 
+  // sum over c < kb of row[c] * w32[k0 + c]: 8 float4 loads for a full block (row 16-byte aligned)
+  __device__ __forceinline__ float row_dot(const float* row, int k0, int kb) const {
+    float acc = 0.f;
+    if (kb == kPW) {
+      float4 a[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) a[q] = *reinterpret_cast<const float4*>(row + 4 * q);
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        acc = fmaf(a[q].x, w32[k0 + 4 * q], acc);
+        acc = fmaf(a[q].y, w32[k0 + 4 * q + 1], acc);
+        acc = fmaf(a[q].z, w32[k0 + 4 * q + 2], acc);
+        acc = fmaf(a[q].w, w32[k0 + 4 * q + 3], acc);
+      }
+    } else {
+      for (int c = 0; c < kb; ++c) acc = fmaf(row[c], w32[k0 + c], acc);
+    }
+    return acc;
+  }
+
   // ---- x = A^-1 b with the factors (FP32 substitutions; b and x FP64 vectors in shared memory)
   // Forward: w = L^-1 (P b), back: x = U^-1 w, by 32-row blocks: the diagonal block by warp 0
   // (one row per lane, shuffles), the rest of the rows as a matrix-vector product over the CTA.
@@ -448,12 +497,7 @@ struct Solver {
         if (lane < kb) w32[r] = val;
       }
       __syncthreads();
-      for (int i = k0 + kb + tid; i < m; i += kNT) {
-        const float* row = A + static_cast<size_t>(perm[i]) * kLda + k0;
-        float acc = 0.f;
-        for (int c = 0; c < kb; ++c) acc = fmaf(row[c], w32[k0 + c], acc);
-        w32[i] -= acc;
-      }
+      for (int i = k0 + kb + tid; i < m; i += kNT) w32[i] -= row_dot(A + static_cast<size_t>(perm[i]) * kLda + k0, k0, kb);
       __syncthreads();
     }
     for (int blk = nb - 1; blk >= 0; --blk) {
@@ -476,12 +520,7 @@ struct Solver {
         if (lane < kb) w32[r] = val;
       }
       __syncthreads();
-      for (int i = tid; i < k0; i += kNT) {
-        const float* row = A + static_cast<size_t>(perm[i]) * kLda + k0;
-        float acc = 0.f;
-        for (int c = 0; c < kb; ++c) acc = fmaf(row[c], w32[k0 + c], acc);
-        w32[i] -= acc;
-      }
+      for (int i = tid; i < k0; i += kNT) w32[i] -= row_dot(A + static_cast<size_t>(perm[i]) * kLda + k0, k0, kb);
       __syncthreads();
     }
     for (int i = tid; i < m; i += kNT) x[i] = static_cast<double>(w32[i]);

@@ -193,8 +193,10 @@ class AtmosphericChemistry:
         ws = torch.zeros(int(n), dtype=torch.uint8, device=state.device)  # error word starts clear
         side = torch.cuda.Stream(device=state.device)
         side.wait_stream(torch.cuda.current_stream(state.device))
-        with torch.cuda.stream(side):  # one eager run: mechanism tables on the device, kernel attributes set
-            t_out.zero_()
+        # one eager call with every sample already past its end (all skipped: no integration work):
+        # mechanism tables on the device, kernel attributes and side streams set up before capture
+        with torch.cuda.stream(side):
+            t_out.fill_(float("inf"))
             AtmosphericChemistry.runDeviceBatch(tol_newton, tol_time, None, tadv, state, t_out, dt_out, state_out,
                                                 kmcd, mech_of_sample=mech_of_sample, status=status, form=form,
                                                 threads_per_sample=threads_per_sample, workspace=ws, stream=side)
