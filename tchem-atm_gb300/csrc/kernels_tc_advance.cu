@@ -40,7 +40,8 @@ constexpr int kNT = 128;                     // threads per CTA (one warpgroup: 
 constexpr int kMaxM = 320;                   // largest system
 constexpr int kLda = 320;                    // row stride of the global matrix (floats)
 constexpr int kPW = 32;                      // panel width = K of the trailing update
-constexpr int kPLd = 33;                     // panel row stride in shared memory (floats)
+constexpr int kPLd = 36;                     // pivot-row stride in shared memory (floats, 16-byte rows)
+constexpr int kRowsPT = (kMaxM + kNT - 1) / kNT;  // panel rows per thread
 constexpr int kMaxTrail = kMaxM - kPW;       // widest trailing matrix
 constexpr int kRowTiles = (kMaxTrail + 127) / 128;
 constexpr int kBTileRows = 288;              // B operand rows (trailing columns, padded to 16)
@@ -55,7 +56,7 @@ size_t tc_advance_smem_bytes(const MechLayout& L) {
   using namespace tcadv;
   auto up128 = [](size_t b) { return (b + 127) & ~size_t(127); };
   size_t b = 1024;                                        // mbarriers, TMEM slot, reductions, flags
-  b += up128(sizeof(float) * kMaxM * kPLd);               // panel
+  b += up128(sizeof(float) * (kPW + 8) * kPLd);           // the panel's pivot rows + pivot candidates
   b += static_cast<size_t>(kRowTiles) * 128 * kPW * 4;    // A operand (L21), K-major
   b += static_cast<size_t>(kBTileRows) * kPW * 4;         // B operand (U12), K-major
   b += up128(sizeof(double) * kNumVec * kMaxM);           // vectors
@@ -77,7 +78,7 @@ __device__ __forceinline__ Layout layout(const MechLayout& L) {
   Layout s;
   uint32_t o = 1024;
   s.panel = o;
-  o += up128(sizeof(float) * kMaxM * kPLd);
+  o += up128(sizeof(float) * (kPW + 8) * kPLd);
   s.aop = o;  // 1024-byte aligned: the operand base offsets below are multiples of 16
   o += kRowTiles * 128 * kPW * 4;
   s.bop = o;
@@ -108,6 +109,8 @@ struct Header {
   double redd[2][4];     // double reductions, two rotating halves
   float redf[2][4];      // pivot candidates |a|
   int32_t redi[2][4];    // pivot candidate rows
+  int32_t pphys[32];     // physical matrix row of the panel's pivot at each step
+  int32_t scnt[3][4];    // non-pivot rows per (row segment, warp): the trailing-order scan
 };
 
 struct Solver {
@@ -116,7 +119,8 @@ struct Solver {
   Header* H;
   SmemTables T;  // the mechanism's tables, read from global memory (L1/L2)
   float* A;      // this CTA's matrix slot [kMaxM][kLda]
-  float* pn;     // panel [kMaxM][kPLd]
+  float* pn;     // the current panel's pivot rows [kPW][kPLd] in step order, then the pivot
+                 // candidates [2][4][kPLd] (step parity, warp)
   unsigned char* aop;
   unsigned char* bop;
   double* vecs;
@@ -127,7 +131,7 @@ struct Solver {
   int32_t* perm;
   int m, R, tid, lane, warp;
   uint32_t tmem;
-  uint32_t ph[2] = {0u, 0u};
+  uint32_t phbits = 0u;  // bit b: the parity to wait for next on TMEM buffer b (a scalar: the struct stays in registers)
   int rr = 0;  // rotating reduction half
   tchem_gb_sample_stats st{};
 
@@ -245,8 +249,9 @@ struct Solver {
 
   // All threads: waits (bounded) for buffer b's MMAs; false when the wait expired anywhere.
   __device__ bool wait_tile(int b) {
-    const bool ok = tc::mbar_wait(&H->mbar[b], ph[b], kSpinLimit);
-    ph[b] ^= 1u;
+    const uint32_t par = (phbits >> b) & 1u;
+    const bool ok = tc::mbar_wait(&H->mbar[b], par, kSpinLimit);
+    phbits ^= 1u << b;
     const bool all = __syncthreads_and(ok ? 1 : 0) != 0;
     if (!all) {
       if (tid == 0) {
@@ -254,7 +259,7 @@ struct Solver {
         H->abort = 1;
       }
       // a second bounded window for the MMAs in flight
-      const bool drained = __syncthreads_and(tc::mbar_wait(&H->mbar[b], ph[b] ^ 1u, kSpinLimit) ? 1 : 0) != 0;
+      const bool drained = __syncthreads_and(tc::mbar_wait(&H->mbar[b], par, kSpinLimit) ? 1 : 0) != 0;
       if (!drained && tid == 0) atomicOr(P.error_word, kErrMmaInFlight);
     }
     tc::fence_after_sync();
@@ -306,89 +311,154 @@ struct Solver {
   __device__ bool lu_factor() {
     for (int k0 = 0; k0 < m; k0 += kPW) {
       const int kb = min(kPW, m - k0), p1 = k0 + kb, np = m - k0;
-      // panel rows k0 .. m-1 (logical), columns k0 .. k0 + 31, into shared memory: 8 float4 per row
-      // (k0 is a multiple of 32 and kLda of 4, so the loads are 16-byte aligned and stay inside the row)
-#pragma unroll 4
-      for (int e = tid; e < np * 8; e += kNT) {
-        const int r = e >> 3, c = 4 * (e & 7);
-        const float4 a = *reinterpret_cast<const float4*>(A + static_cast<size_t>(perm[k0 + r]) * kLda + k0 + c);
-        float* d = pn + r * kPLd + c;
-        d[0] = c < kb ? a.x : 0.f;
-        d[1] = c + 1 < kb ? a.y : 0.f;
-        d[2] = c + 2 < kb ? a.z : 0.f;
-        d[3] = c + 3 < kb ? a.w : 0.f;
+      // The panel (logical rows k0 .. m-1, columns k0 .. k0 + 31) in registers, panel row
+      // r = tid + 128 s held by thread tid. Implicit pivoting: the pivot row of each step is
+      // published to shared memory (pn row c = L11 row c left of the diagonal, U11 row c from it)
+      // and leaves the active set; the other rows are updated in registers. k0 is a multiple of
+      // 32 and kLda of 4, so the float4 loads are aligned and stay inside the row.
+      float a[kRowsPT][kPW];
+      bool act[kRowsPT];
+      int prow[kRowsPT];
+#pragma unroll
+      for (int s = 0; s < kRowsPT; ++s) {
+        const int r = tid + kNT * s;
+        act[s] = r < np;
+        prow[s] = act[s] ? perm[k0 + r] : 0;
+#pragma unroll
+        for (int q = 0; q < kPW / 4; ++q) {
+          float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+          if (act[s]) v = *reinterpret_cast<const float4*>(A + static_cast<size_t>(prow[s]) * kLda + k0 + 4 * q);
+          a[s][4 * q] = 4 * q < kb ? v.x : 0.f;
+          a[s][4 * q + 1] = 4 * q + 1 < kb ? v.y : 0.f;
+          a[s][4 * q + 2] = 4 * q + 2 < kb ? v.z : 0.f;
+          a[s][4 * q + 3] = 4 * q + 3 < kb ? v.w : 0.f;
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < kPW; ++c) {
+        if (c < kb) {  // uniform
+          // Pivot with one barrier: a packed key per row (|a| with its low 9 mantissa bits replaced
+          // by 511 - panel row, so one max picks the largest magnitude to a relative 2^-14, ties to
+          // the lowest row), one redux per warp; each warp's winning lane writes its row to the
+          // warp's candidate slot (double-buffered by step parity) and lane 0 the warp's key.
+          uint32_t key = 0u;
+#pragma unroll
+          for (int s = 0; s < kRowsPT; ++s) {
+            const uint32_t kb9 = (__float_as_uint(a[s][c]) & 0x7fffffffu & ~511u) |
+                                 (511u - static_cast<uint32_t>(tid + kNT * s));
+            key = max(key, act[s] ? kb9 : 0u);
+          }
+          const uint32_t wkey = __reduce_max_sync(kFullMask, key);
+          const int par = c & 1;
+          float* cand = pn + (kPW + 4 * par + warp) * kPLd;
+          if (key == wkey && wkey != 0u) {
+            const int so = static_cast<int>(511u - (wkey & 511u)) / kNT;
+#pragma unroll
+            for (int s = 0; s < kRowsPT; ++s)
+              if (s == so) {
+#pragma unroll
+                for (int q = 0; q < kPW / 4; ++q)
+                  *reinterpret_cast<float4*>(cand + 4 * q) =
+                      make_float4(a[s][4 * q], a[s][4 * q + 1], a[s][4 * q + 2], a[s][4 * q + 3]);
+              }
+          }
+          uint32_t* keys = reinterpret_cast<uint32_t*>(H->redi[par]);
+          if (lane == 0) keys[warp] = wkey;
+          __syncthreads();
+          uint32_t best = keys[0];
+          int bw = 0;
+#pragma unroll
+          for (int w = 1; w < 4; ++w)
+            if (keys[w] > best) {
+              best = keys[w];
+              bw = w;
+            }
+          const uint32_t mag = best & ~511u;
+          if (mag == 0u || mag >= 0x7f800000u) return false;  // zero column, inf or nan (uniform)
+          const int bi = static_cast<int>(511u - (best & 511u));  // the pivot's panel row
+          const float* prow_s = pn + (kPW + 4 * par + bw) * kPLd;
+          float u[kPW];
+#pragma unroll
+          for (int q = 0; q < kPW / 4; ++q) {
+            const float4 v = *reinterpret_cast<const float4*>(prow_s + 4 * q);
+            u[4 * q] = v.x;
+            u[4 * q + 1] = v.y;
+            u[4 * q + 2] = v.z;
+            u[4 * q + 3] = v.w;
+          }
+          if ((bi & (kNT - 1)) == tid) {  // the owner records the step and drops the row
+            const int so = bi / kNT;
+#pragma unroll
+            for (int s = 0; s < kRowsPT; ++s)
+              if (s == so) {
+#pragma unroll
+                for (int q = 0; q < kPW / 4; ++q)
+                  *reinterpret_cast<float4*>(pn + c * kPLd + 4 * q) =
+                      make_float4(a[s][4 * q], a[s][4 * q + 1], a[s][4 * q + 2], a[s][4 * q + 3]);
+                act[s] = false;
+                H->pphys[c] = prow[s];
+              }
+          }
+          const float inv = 1.f / u[c];
+#pragma unroll
+          for (int s = 0; s < kRowsPT; ++s) {
+            if (act[s]) {
+              const float l = a[s][c] * inv;
+              a[s][c] = l;
+#pragma unroll
+              for (int j = c + 1; j < kPW; ++j) a[s][j] = fmaf(-l, u[j], a[s][j]);
+            }
+          }
+        }
+      }
+      __syncthreads();  // pivot rows (pn) and pphys complete
+      // factored rows back to the matrix (physical rows): L and U11 of the pivot rows, L21
+#pragma unroll
+      for (int s = 0; s < kRowsPT; ++s) {
+        if (tid + kNT * s < np) {
+          float* dst = A + static_cast<size_t>(prow[s]) * kLda + k0;
+#pragma unroll
+          for (int q = 0; q < kPW / 4; ++q) {
+            if (4 * q + 4 <= kb) {
+              *reinterpret_cast<float4*>(dst + 4 * q) =
+                  make_float4(a[s][4 * q], a[s][4 * q + 1], a[s][4 * q + 2], a[s][4 * q + 3]);
+            } else {
+#pragma unroll
+              for (int z = 0; z < 4; ++z)
+                if (4 * q + z < kb) dst[4 * q + z] = a[s][4 * q + z];
+            }
+          }
+        }
+      }
+      // trailing order: the non-pivot rows by increasing panel row (an exclusive scan of the
+      // still-active flags over r = tid + 128 s)
+      int qpos[kRowsPT];
+#pragma unroll
+      for (int s = 0; s < kRowsPT; ++s) {
+        const unsigned bal = __ballot_sync(kFullMask, act[s]);
+        qpos[s] = __popc(bal & ((1u << lane) - 1u));
+        if (lane == 0) H->scnt[s][warp] = __popc(bal);
       }
       __syncthreads();
-      for (int c = 0; c < kb; ++c) {
-        // pivot: first largest |a| among logical rows k0 + c .. m - 1
-        float best = -1.f;
-        int bi = np;
-        for (int r = c + tid; r < np; r += kNT) {
-          const float a = fabsf(pn[r * kPLd + c]);
-          if (a > best) {
-            best = a;
-            bi = r;
-          }
-        }
+      {
+        int base = 0;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          const float ob = __shfl_xor_sync(kFullMask, best, o);
-          const int oi = __shfl_xor_sync(kFullMask, bi, o);
-          if (ob > best || (ob == best && oi < bi)) {
-            best = ob;
-            bi = oi;
-          }
-        }
-        float* rv = H->redf[rr];
-        int* ri = H->redi[rr];
-        rr ^= 1;
-        if (lane == 0) {
-          rv[warp] = best;
-          ri[warp] = bi;
-        }
-        __syncthreads();
-        best = rv[0];
-        bi = ri[0];
+        for (int s = 0; s < kRowsPT; ++s) {
+          int off = base;
 #pragma unroll
-        for (int w = 1; w < 4; ++w)
-          if (rv[w] > best || (rv[w] == best && ri[w] < bi)) {
-            best = rv[w];
-            bi = ri[w];
+          for (int w = 0; w < 4; ++w) {
+            if (w < warp) off += H->scnt[s][w];
+            base += H->scnt[s][w];
           }
-        if (!(best > 0.f) || !isfinite(best) || bi >= np) return false;  // uniform
-        if (bi != c) {
-          if (tid < kPW) {
-            const float t = pn[c * kPLd + tid];
-            pn[c * kPLd + tid] = pn[bi * kPLd + tid];
-            pn[bi * kPLd + tid] = t;
-          }
-          if (tid == kPW) {
-            const int t = perm[k0 + c];
-            perm[k0 + c] = perm[k0 + bi];
-            perm[k0 + bi] = t;
-          }
-          __syncthreads();
-        }
-        const float inv = 1.f / pn[c * kPLd + c];
-        for (int r = c + 1 + tid; r < np; r += kNT) {
-          const float l = pn[r * kPLd + c] * inv;
-          pn[r * kPLd + c] = l;
-          for (int j = c + 1; j < kb; ++j) pn[r * kPLd + j] = fmaf(-l, pn[c * kPLd + j], pn[r * kPLd + j]);
-        }
-        __syncthreads();
-      }
-      // the factored panel back to the matrix (physical rows), 8 float4 per row
-#pragma unroll 4
-      for (int e = tid; e < np * 8; e += kNT) {
-        const int r = e >> 3, c = 4 * (e & 7);
-        float* dst = A + static_cast<size_t>(perm[k0 + r]) * kLda + k0 + c;
-        const float* src = pn + r * kPLd + c;
-        if (c + 4 <= kb) {
-          *reinterpret_cast<float4*>(dst) = make_float4(src[0], src[1], src[2], src[3]);
-        } else {
-          for (int z = 0; c + z < kb; ++z) dst[z] = src[z];
+          qpos[s] += off;
         }
       }
+      // the new logical order: the kb pivots, then the trailing rows
+      if (tid < kb) perm[k0 + tid] = H->pphys[tid];
+#pragma unroll
+      for (int s = 0; s < kRowsPT; ++s)
+        if (act[s]) perm[p1 + qpos[s]] = prow[s];
+      __syncthreads();  // the new order before U12 reads the pivot rows through it
       const int W = m - p1;  // trailing width
       if (W <= 0) break;
       const int N0 = W <= 256 ? ((W + 15) & ~15) : (((W + 1) / 2 + 15) & ~15);
@@ -405,7 +475,13 @@ struct Solver {
         for (int i = 1; i < kPW; ++i) {
           float acc = u[i];
 #pragma unroll
-          for (int l = 0; l < i; ++l) acc = fmaf(-pn[i * kPLd + l], u[l], acc);
+          for (int q = 0; 4 * q < i; ++q) {  // L11 row i, columns 0 .. i-1, as float4 reads
+            const float4 v = *reinterpret_cast<const float4*>(pn + i * kPLd + 4 * q);
+            acc = fmaf(-v.x, u[4 * q], acc);
+            if (4 * q + 1 < i) acc = fmaf(-v.y, u[4 * q + 1], acc);
+            if (4 * q + 2 < i) acc = fmaf(-v.z, u[4 * q + 2], acc);
+            if (4 * q + 3 < i) acc = fmaf(-v.w, u[4 * q + 3], acc);
+          }
           u[i] = i < kb ? acc : 0.f;
         }
 #pragma unroll
@@ -414,12 +490,19 @@ struct Solver {
           *reinterpret_cast<float*>(bop + tc::kmajor_offset(j, i, kPW)) = u[i];
         }
       }
-      // L21 (panel rows kb .. np-1) as the A operand, zero rows beyond the trailing matrix
+      // L21 (the trailing rows' multipliers, from registers) as the A operand; rows W .. of the last
+      // 128-row tile are zero
       const int nrt = (W + 127) / 128;
-      for (int e = tid; e < nrt * 128 * kPW; e += kNT) {
+#pragma unroll
+      for (int s = 0; s < kRowsPT; ++s)
+        if (act[s]) {
+#pragma unroll
+          for (int c = 0; c < kPW; ++c)
+            *reinterpret_cast<float*>(aop + tc::kmajor_offset(qpos[s], c, kPW)) = c < kb ? a[s][c] : 0.f;
+        }
+      for (int e = W * kPW + tid; e < nrt * 128 * kPW; e += kNT) {
         const int r = e / kPW, c = e - r * kPW;
-        const float a = (r < W && c < kb) ? pn[(kb + r) * kPLd + c] : 0.f;
-        *reinterpret_cast<float*>(aop + tc::kmajor_offset(r, c, kPW)) = a;
+        *reinterpret_cast<float*>(aop + tc::kmajor_offset(r, c, kPW)) = 0.f;
       }
       tc::fence_proxy_async();  // generic-proxy operand writes before the MMAs read them
       tc::fence_before_sync();
@@ -437,7 +520,8 @@ struct Solver {
         if (!wait_tile(j & 1)) {
           // the buffer of tile j + 1 may still be in flight: give it the second window too
           if (j + 1 < nt) {
-            const bool d = __syncthreads_and(tc::mbar_wait(&H->mbar[(j + 1) & 1], ph[(j + 1) & 1], kSpinLimit) ? 1 : 0);
+            const int b1 = (j + 1) & 1;
+            const bool d = __syncthreads_and(tc::mbar_wait(&H->mbar[b1], (phbits >> b1) & 1u, kSpinLimit) ? 1 : 0);
             if (!d && tid == 0) atomicOr(P.error_word, kErrMmaInFlight);
           }
           return false;
@@ -474,53 +558,73 @@ struct Solver {
   }
 
   // ---- x = A^-1 b with the factors (FP32 substitutions; b and x FP64 vectors in shared memory)
-  // Forward: w = L^-1 (P b), back: x = U^-1 w, by 32-row blocks: the diagonal block by warp 0
-  // (one row per lane, shuffles), the rest of the rows as a matrix-vector product over the CTA.
+  // Forward: w = L^-1 (P b), back: x = U^-1 w, by 32-row blocks. Warp 0 applies the previous
+  // block to the next block's rows and then solves that block (one row per lane, shuffles) while
+  // warps 1-3 apply the previous block to the remaining rows: one barrier per block.
+  __device__ void diag_lower(int k0) {  // warp 0: unit-lower diagonal block at k0
+    const int kb = min(kPW, m - k0), r = k0 + lane;
+    float lrow[kPW];
+    const float* src = A + static_cast<size_t>(perm[r < m ? r : k0]) * kLda + k0;
+#pragma unroll
+    for (int c = 0; c < kPW; ++c) lrow[c] = (r < m && c < kb) ? src[c] : 0.f;
+    float val = r < m ? w32[r] : 0.f;
+#pragma unroll
+    for (int c = 0; c < kPW; ++c) {
+      const float zc = __shfl_sync(kFullMask, val, c);
+      if (lane > c) val = fmaf(-lrow[c], zc, val);
+    }
+    if (lane < kb) w32[r] = val;
+  }
+  __device__ void diag_upper(int k0) {  // warp 0: upper diagonal block at k0
+    const int kb = min(kPW, m - k0), r = k0 + lane;
+    float urow[kPW];
+    const float* src = A + static_cast<size_t>(perm[r < m ? r : k0]) * kLda + k0;
+#pragma unroll
+    for (int c = 0; c < kPW; ++c) urow[c] = (r < m && c < kb) ? src[c] : 0.f;
+    float val = r < m ? w32[r] : 0.f;
+#pragma unroll
+    for (int c = kPW - 1; c >= 0; --c) {
+      if (c < kb) {
+        if (lane == c) val = val / urow[c];
+        const float xc = __shfl_sync(kFullMask, val, c);
+        if (lane < c) val = fmaf(-urow[c], xc, val);
+      }
+    }
+    if (lane < kb) w32[r] = val;
+  }
+
   __device__ void solve(const double* b, double* x) {
     for (int i = tid; i < m; i += kNT) w32[i] = static_cast<float>(b[perm[i]]);
     __syncthreads();
     const int nb = (m + kPW - 1) / kPW;
-    for (int blk = 0; blk < nb; ++blk) {
-      const int k0 = blk * kPW, kb = min(kPW, m - k0);
+    if (warp == 0) diag_lower(0);
+    __syncthreads();
+    for (int blk = 0; blk + 1 < nb; ++blk) {
+      const int k0 = blk * kPW, next = k0 + kPW;  // block blk is full (32 rows): it is not the last
       if (warp == 0) {
-        const int r = k0 + lane;
-        float lrow[kPW];
-        const float* src = A + static_cast<size_t>(perm[r < m ? r : k0]) * kLda + k0;
-#pragma unroll
-        for (int c = 0; c < kPW; ++c) lrow[c] = (r < m && c < kb) ? src[c] : 0.f;
-        float val = r < m ? w32[r] : 0.f;
-#pragma unroll
-        for (int c = 0; c < kPW; ++c) {
-          const float zc = __shfl_sync(kFullMask, val, c);
-          if (lane > c) val = fmaf(-lrow[c], zc, val);
-        }
-        if (lane < kb) w32[r] = val;
+        const int r = next + lane;
+        if (r < m) w32[r] -= row_dot(A + static_cast<size_t>(perm[r]) * kLda + k0, k0, kPW);
+        __syncwarp();
+        diag_lower(next);
+      } else {
+        for (int i = next + kPW + (tid - 32); i < m; i += kNT - 32)
+          w32[i] -= row_dot(A + static_cast<size_t>(perm[i]) * kLda + k0, k0, kPW);
       }
-      __syncthreads();
-      for (int i = k0 + kb + tid; i < m; i += kNT) w32[i] -= row_dot(A + static_cast<size_t>(perm[i]) * kLda + k0, k0, kb);
       __syncthreads();
     }
-    for (int blk = nb - 1; blk >= 0; --blk) {
-      const int k0 = blk * kPW, kb = min(kPW, m - k0);
+    if (warp == 0) diag_upper((nb - 1) * kPW);
+    __syncthreads();
+    for (int blk = nb - 1; blk > 0; --blk) {
+      const int k0 = blk * kPW, kb = min(kPW, m - k0), prev = k0 - kPW;
       if (warp == 0) {
-        const int r = k0 + lane;
-        float urow[kPW];
-        const float* src = A + static_cast<size_t>(perm[r < m ? r : k0]) * kLda + k0;
-#pragma unroll
-        for (int c = 0; c < kPW; ++c) urow[c] = (r < m && c < kb) ? src[c] : 0.f;
-        float val = r < m ? w32[r] : 0.f;
-#pragma unroll
-        for (int c = kPW - 1; c >= 0; --c) {
-          if (c < kb) {
-            if (lane == c) val = val / urow[c];
-            const float xc = __shfl_sync(kFullMask, val, c);
-            if (lane < c) val = fmaf(-urow[c], xc, val);
-          }
-        }
-        if (lane < kb) w32[r] = val;
+        const int r = prev + lane;
+        w32[r] -= row_dot(A + static_cast<size_t>(perm[r]) * kLda + k0, k0, kb);
+        __syncwarp();
+        diag_upper(prev);
+      } else {
+        for (int i = tid - 32; i < prev; i += kNT - 32)
+          w32[i] -= row_dot(A + static_cast<size_t>(perm[i]) * kLda + k0, k0, kb);
       }
-      __syncthreads();
-      for (int i = tid; i < k0; i += kNT) w32[i] -= row_dot(A + static_cast<size_t>(perm[i]) * kLda + k0, k0, kb);
       __syncthreads();
     }
     for (int i = tid; i < m; i += kNT) x[i] = static_cast<double>(w32[i]);
