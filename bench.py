@@ -958,9 +958,9 @@ def engine_arm(args, world: int, rank: int, local: int):
 
     legs = [("e3sm", args.e3sm_samples, lambda n: e3sm_leg(n, min(args.cpu_seconds, 5.0), dev, stream)),
             ("large_mechanism", args.large_samples, lambda n: large_leg(n, args.large_horizon, dev, stream)),
+            ("aerosol", args.aerosol_samples, lambda n: aerosol_leg(n, min(args.cpu_seconds, 5.0), dev, stream)),
             ("uneven_batch", args.uneven_samples, lambda n: uneven_leg(n, args.form, dev, stream)),
             ("adjoint", args.adjoint_samples, lambda n: adjoint_leg(km, state, tol_time, n, dev, stream)),
-            ("aerosol", args.aerosol_samples, lambda n: aerosol_leg(n, min(args.cpu_seconds, 5.0), dev, stream)),
             ("tc_lu", args.tc_lu_matrices, lambda n: tc_lu_leg(n, dev, stream))]
     for key, n, fn in legs:
         if rank == 0 and n > 0:
