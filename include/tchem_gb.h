@@ -164,6 +164,17 @@ int tchem_gb_mech_host_view(const tchem_gb_mech* mech, tchem_gb_kmcd_view* view)
 int tchem_gb_mech_e3sm_view(const tchem_gb_mech* mech, tchem_gb_e3sm_view* view);
 /* Copies species name i (truncated as the reference stores it) into buf. */
 int tchem_gb_mech_species_name(const tchem_gb_mech* mech, int i, char* buf, int buflen);
+/* The static-order sparse LU of the mechanism's Newton matrix (no counterpart in the reference,
+ * whose Tines solve factors the dense matrix with partial pivoting): the elimination program the
+ * full-Newton FP32 form's one-warp shape runs for 33 to 128 active species. info[12] receives
+ * m, nnz (entries of the filled pattern), n_ops (trailing updates), prog_len and the offsets
+ * (int32 units into prog) of diag[m], pos[m], lc_ptr[m+1], lc[], uc_ptr[m+1], uc[], up_ptr[m+1]
+ * and up[2 n_ops]: pos[s] is the elimination position of species s; diag[k] the entry of (k, k);
+ * lc / uc list column k of L below / U above the diagonal as entry | row << 16; up holds step k's
+ * updates as pairs (dst | l << 16, u): a[dst] -= a[l] * a[u]. Entries number the filled pattern
+ * row-major in position order. prog (may be NULL) receives min(prog_cap, prog_len) values.
+ * TCHEM_GB_ERR_UNSUPPORTED for mechanisms above 128 active species. */
+int tchem_gb_mech_sparse_lu(const tchem_gb_mech* mech, int32_t* info, int32_t* prog, int prog_cap);
 
 /* Scenario file -> state[nbatch][nSpec+3] on the host ([rho, p, T, x...]). */
 int tchem_gb_scenario_batch_size(const char* yaml_path, int* nbatch);

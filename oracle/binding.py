@@ -20,6 +20,8 @@ def load(native: bool = False) -> C.CDLL:
         vp = C.c_void_p
         L.oracle_set_lu_tile_bits.restype = C.c_int
         L.oracle_set_lu_tile_bits.argtypes = [C.c_int]
+        L.oracle_set_lu_static_order.restype = C.c_int
+        L.oracle_set_lu_static_order.argtypes = [C.c_int, C.c_void_p]
         L.oracle_lu_factor_blocked.restype = C.c_int
         L.oracle_lu_factor_blocked.argtypes = [C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
         L.oracle_kforward.restype = C.c_int

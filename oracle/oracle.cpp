@@ -257,6 +257,12 @@ void jacobian(const tchem_gb_kmcd_view& km, const double* kfor, const double* co
 // (oracle_set_lu_tile_bits): 0 = unblocked FP32 LU; 10 = TF32 tiles, 7 = BF16 tiles.
 int g_lu_tile_bits = 0;
 
+// Static symmetric elimination order without pivoting for FP32 factorizations of matrices of its
+// size (oracle_set_lu_static_order): row and column k of the factored matrix are species
+// g_lu_order[k]. A sparse factorization in that order performs exactly these operations on the
+// structural nonzeros (the skipped ones only ever add 0 to 0).
+std::vector<int> g_lu_order;
+
 // Round-to-nearest-even of an FP32 value to `keep` mantissa bits (TF32: 10, BF16: 7).
 float round_mantissa(float x, int keep) {
   uint32_t u;
@@ -278,8 +284,11 @@ struct DenseLU {
   std::vector<T> a;
   std::vector<int> piv;
   std::vector<T> w;
+  std::vector<T> dinv;   // ordered factors: reciprocals of the pivots
+  bool ordered = false;  // the factors are of the static order (g_lu_order)
   void resize(int n_) {
     n = n_;
+    dinv.assign(n_, T(0));
     a.assign(static_cast<size_t>(n) * n, T(0));
     piv.assign(n, 0);
     w.assign(n, T(0));
@@ -328,6 +337,8 @@ struct DenseLU {
   }
   // A = I - c J, built in double and rounded to T.
   bool factor(const double* J, double c) {
+    ordered = sizeof(T) == 4 && static_cast<int>(g_lu_order.size()) == n;
+    if (ordered) return factor_ordered(J, c);
     for (int i = 0; i < n; ++i)
       for (int j = 0; j < n; ++j)
         a[static_cast<size_t>(i) * n + j] = static_cast<T>((i == j ? 1.0 : 0.0) - c * J[static_cast<size_t>(i) * n + j]);
@@ -365,8 +376,49 @@ struct DenseLU {
       if (piv[k] != k) std::swap(w[k], w[piv[k]]);
     for (int i = 0; i < n; ++i) x[i] = static_cast<double>(w[i]);
   }
+  // P (I - c J) P^T = L U with P the static order, no row exchanges.
+  bool factor_ordered(const double* J, double c) {
+    const int* o = g_lu_order.data();
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j)
+        a[static_cast<size_t>(i) * n + j] =
+            static_cast<T>((o[i] == o[j] ? 1.0 : 0.0) - c * J[static_cast<size_t>(o[i]) * n + o[j]]);
+    for (int k = 0; k < n; ++k) {
+      piv[k] = k;
+      const T akk = a[static_cast<size_t>(k) * n + k];
+      if (!(std::abs(akk) > T(0)) || !std::isfinite(static_cast<double>(akk))) return false;
+      const T inv = T(1) / akk;
+      dinv[k] = inv;
+      for (int i = k + 1; i < n; ++i) {
+        const T l = a[static_cast<size_t>(i) * n + k] * inv;
+        a[static_cast<size_t>(i) * n + k] = l;
+        for (int j = k + 1; j < n; ++j) a[static_cast<size_t>(i) * n + j] -= l * a[static_cast<size_t>(k) * n + j];
+      }
+    }
+    return true;
+  }
+  // Column-oriented substitutions of the ordered factors on w: L z = w, then U x = z with
+  // x_k = z_k * (1 / u_kk) and the column of x_k eliminated from the rows above.
+  void substitute() {
+    for (int k = 0; k < n; ++k) {
+      const T wk = w[k];
+      for (int i = k + 1; i < n; ++i) w[i] -= a[static_cast<size_t>(i) * n + k] * wk;
+    }
+    for (int k = n - 1; k >= 0; --k) {
+      const T xk = w[k] * dinv[k];
+      w[k] = xk;
+      for (int i = 0; i < k; ++i) w[i] -= a[static_cast<size_t>(i) * n + k] * xk;
+    }
+  }
   // x = A^{-1} b (b and x in double, arithmetic in T).
   void solve(const double* b, double* x) {
+    if (ordered) {
+      const int* o = g_lu_order.data();
+      for (int k = 0; k < n; ++k) w[k] = static_cast<T>(b[o[k]]);
+      substitute();
+      for (int k = 0; k < n; ++k) x[o[k]] = static_cast<double>(w[k]);
+      return;
+    }
     for (int i = 0; i < n; ++i) w[i] = static_cast<T>(b[i]);
     for (int k = 0; k < n; ++k)
       if (piv[k] != k) std::swap(w[k], w[piv[k]]);
@@ -910,6 +962,18 @@ int oracle_lu_factor_blocked(int n, const float* a_in, int keep, float* lu, int3
 int oracle_set_lu_tile_bits(int bits) {
   if (bits != 0 && (bits < 1 || bits > 23)) return TCHEM_GB_ERR_ARG;
   g_lu_tile_bits = bits;
+  return TCHEM_GB_OK;
+}
+
+// Static elimination order of FP32 factorizations of n x n matrices (n = 0: partial pivoting).
+int oracle_set_lu_static_order(int n, const int32_t* order) {
+  if (n < 0 || (n > 0 && !order)) return TCHEM_GB_ERR_ARG;
+  std::vector<int> o(order, order + n), seen(n, 0);
+  for (int k = 0; k < n; ++k) {
+    if (o[k] < 0 || o[k] >= n || seen[o[k]]) return TCHEM_GB_ERR_ARG;
+    seen[o[k]] = 1;
+  }
+  g_lu_order = o;
   return TCHEM_GB_OK;
 }
 

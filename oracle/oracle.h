@@ -37,6 +37,10 @@ extern "C" {
  * panels in FP32 and the trailing update with operands rounded to `bits` mantissa bits (10: TF32,
  * 7: BF16) and FP32 accumulation; 0 (default): the unblocked FP32 LU. A process-wide setting. */
 int oracle_set_lu_tile_bits(int bits);
+/* FP32 factorizations of n x n Newton matrices in a static symmetric order without pivoting, as a
+ * sparse factorization computes them: row and column k are species order[k]; the substitutions are
+ * column-oriented with the pivots' reciprocals. n = 0 restores partial pivoting. Process-wide. */
+int oracle_set_lu_static_order(int n, const int32_t* order);
 /* One FP32 matrix a[n][n] factored as the tensor-core LU does: 32-column panels with partial
  * pivoting, trailing update on operands rounded to `keep` mantissa bits (10: TF32, 23: none);
  * lu[n][n] and piv[n] as LAPACK's sgetrf (0-based pivots). */

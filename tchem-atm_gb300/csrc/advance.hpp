@@ -17,6 +17,7 @@ constexpr int kTapeSegment = 32;    // steps between trajectory checkpoints (adj
 struct MixedLayout {
   uint32_t warp_bytes;
   uint32_t x, keff, q, x32, keff32, d32, ustage, lrow, pinv, piv, ybuf, vec, stats, red, item;
+  uint32_t lu;   // [nnz] FP32 factors of the sparse-LU shape (else 0)
   uint32_t src;  // [m] the sample's E3SM source term (E3SM instantiations only; else 0)
   int32_t LDU, LDL;
   int32_t simplified;  // 1: simplified-Newton form; 2: full Newton on the Gauss-Jordan inverse; 0: LU

@@ -240,7 +240,8 @@ Plan make_plan(const tchem_gb_mech* const* mechs, int n_mechs, int nbatch, bool 
       int tps = o.threads_per_sample;
       if (tps == 0 && o.form >= 0 && o.form < 3) tps = mechs[g.mechs[0]]->tps_pref[o.form];
       MixedConfig mc = mixed_config(L, tps, info.sm_count, info.max_smem_optin, nbatch,
-                                    o.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED, e3sm);
+                                    o.form == TCHEM_GB_FORM_MIXED_SIMPLIFIED, e3sm,
+                                    g.dev.lu_prog ? g.dev.lu.nnz : 0);
       g.kernel = mc.kernel;
       g.warps_per_block = mc.warps_per_block;
       g.grid = mc.grid;

@@ -1,4 +1,5 @@
 // C ABI: mechanism and scenario entry points (host only).
+#include <algorithm>
 #include <cctype>
 #include <cstring>
 #include <fstream>
@@ -194,6 +195,34 @@ int tchem_gb_mech_species_name(const tchem_gb_mech* mech, int i, char* buf, int 
   }
   std::strncpy(buf, mech->km.speciesNames[i].c_str(), static_cast<size_t>(buflen) - 1);
   buf[buflen - 1] = '\0';
+  return TCHEM_GB_OK;
+}
+
+int tchem_gb_mech_sparse_lu(const tchem_gb_mech* mech, int32_t* info, int32_t* prog, int prog_cap) {
+  if (!mech || !info || prog_cap < 0) {
+    set_last_error("tchem_gb_mech_sparse_lu: bad argument");
+    return TCHEM_GB_ERR_ARG;
+  }
+  auto* mm = const_cast<tchem_gb_mech*>(mech);
+  {
+    std::lock_guard<std::mutex> lk(mm->mu);
+    try {
+      if (!mm->host_tables) mm->host_tables.reset(new tchem_gb::HostTables(tchem_gb::build_host_tables(mm->km)));
+    } catch (const std::exception& e) {
+      set_last_error(e.what());
+      return TCHEM_GB_ERR_ARG;
+    }
+  }
+  const tchem_gb::SparseLuHost& h = mm->host_tables->slu;
+  if (h.lay.m == 0) {
+    set_last_error("tchem_gb_mech_sparse_lu: no sparse LU program (more than 128 active species)");
+    return TCHEM_GB_ERR_UNSUPPORTED;
+  }
+  const tchem_gb::SparseLuLayout& L = h.lay;
+  const int32_t v[12] = {L.m, L.nnz, L.n_ops, L.prog_len, L.off_diag, L.off_pos,
+                         L.off_lc_ptr, L.off_lc, L.off_uc_ptr, L.off_uc, L.off_up_ptr, L.off_up};
+  std::memcpy(info, v, sizeof(v));
+  if (prog) std::memcpy(prog, h.prog.data(), sizeof(int32_t) * std::min<size_t>(prog_cap, h.prog.size()));
   return TCHEM_GB_OK;
 }
 

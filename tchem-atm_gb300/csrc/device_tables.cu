@@ -286,6 +286,7 @@ HostTables build_host_tables(const KineticModel& km) {
   L.off_rf_sp = sec(sizeof(int16_t) * rf_sp.size());
   L.off_pr_r = sec(sizeof(int16_t) * pr_r.size());
   L.off_jc_f = sec(sizeof(int16_t) * jc_f.size());
+  L.off_js_e = -1;
   L.blob_bytes = static_cast<int32_t>(align16(off));
   ht.blob.assign(L.blob_bytes, 0);
   put(ht.blob, L.off_emis, emis);
@@ -311,6 +312,18 @@ HostTables build_host_tables(const KineticModel& km) {
     std::vector<int32_t> wids(m);
     for (int k = 0; k < m; ++k) wids[k] = k;
     const Sliced js = make_slices(jlists, jids, static_cast<int16_t>(L.NF));
+    // sparse-LU entry of every Jacobian slot (padding lanes: 0, never written)
+    std::vector<int16_t> js_e;
+    if (m <= kSparseLuMaxSpecies) {
+      std::vector<std::pair<int, int>> nz;
+      for (const auto& kv : jac) nz.push_back(kv.first);
+      ht.slu = build_sparse_lu(m, nz);
+      for (int32_t rc : js.item) {
+        int e = 0;
+        if (rc >= 0) e = ht.slu.entry[static_cast<size_t>(ht.slu.pos[rc >> 16]) * m + ht.slu.pos[rc & 0xffff]];
+        js_e.push_back(static_cast<int16_t>(e));
+      }
+    }
     const Sliced ws = make_slices(per_species, wids, static_cast<int16_t>(R));
     std::vector<float> jse_nu32(js.val.begin(), js.val.end());
     MechLayout& X = ht.Lx;
@@ -334,6 +347,7 @@ HostTables build_host_tables(const KineticModel& km) {
     X.off_rf_sp = sx(sizeof(int16_t) * rf_sp.size());
     X.off_jse_f = sx(sizeof(int16_t) * js.idx.size());
     X.off_wse_r = sx(sizeof(int16_t) * ws.idx.size());
+    X.off_js_e = js_e.empty() ? -1 : sx(sizeof(int16_t) * js_e.size());
     // CSR sections are not part of the mixed blob
     X.off_pr_ptr = X.off_pr_r = X.off_pr_nu = X.off_jz_rc = X.off_jz_ptr = X.off_jc_f = X.off_jc_nu = X.off_jc_nu32 = -1;
     X.blob_bytes = static_cast<int32_t>(align16(o));
@@ -351,6 +365,7 @@ HostTables build_host_tables(const KineticModel& km) {
     put(ht.blob_x, X.off_ws_off, ws.off);
     put(ht.blob_x, X.off_wse_r, ws.idx);
     put(ht.blob_x, X.off_wse_nu, ws.val);
+    if (!js_e.empty()) put(ht.blob_x, X.off_js_e, js_e);
   }
 
   // Structural signature: everything except the rate parameters.
@@ -385,6 +400,7 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   const size_t o_e3a = sec(sizeof(int32_t) * std::max<size_t>(1, ht.e3_adj_sp.size()));
   const size_t o_e3o = sec(sizeof(int32_t) * std::max<size_t>(1, ht.e3_o1d.size()));
   const size_t o_e3op = sec(sizeof(double) * std::max<size_t>(1, ht.e3_o1d_par.size()));
+  const size_t o_lu = sec(sizeof(int32_t) * std::max<size_t>(1, ht.slu.prog.size()));
   std::vector<unsigned char> host(off, 0);
   std::memcpy(host.data() + o_blob, ht.blob.data(), ht.blob.size());
   std::memcpy(host.data() + o_blob_x, ht.blob_x.data(), ht.blob_x.size());
@@ -404,6 +420,8 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   if (!ht.e3_o1d.empty()) std::memcpy(host.data() + o_e3o, ht.e3_o1d.data(), sizeof(int32_t) * ht.e3_o1d.size());
   if (!ht.e3_o1d_par.empty())
     std::memcpy(host.data() + o_e3op, ht.e3_o1d_par.data(), sizeof(double) * ht.e3_o1d_par.size());
+  if (!ht.slu.prog.empty())
+    std::memcpy(host.data() + o_lu, ht.slu.prog.data(), sizeof(int32_t) * ht.slu.prog.size());
 
   int prev = 0;
   cudaGetDevice(&prev);
@@ -444,6 +462,8 @@ DeviceTables* upload_tables(const HostTables& ht, int device) {
   t->dev.e3_o1d_par = reinterpret_cast<const double*>(b + o_e3op);
   t->dev.e3_no1d = static_cast<int32_t>(ht.e3_o1d.size() / 7);
   t->dev.M_index = ht.M_index;
+  t->dev.lu_prog = ht.slu.prog.empty() ? nullptr : reinterpret_cast<const int32_t*>(b + o_lu);
+  t->dev.lu = ht.slu.lay;
   t->dev_x = t->dev;
   t->dev_x.L = ht.Lx;
   t->dev_x.blob = b + o_blob_x;

@@ -21,6 +21,7 @@
 #include <vector>
 
 #include "kinetic_model.hpp"
+#include "sparse_lu.hpp"
 
 namespace tchem_gb {
 
@@ -48,6 +49,9 @@ struct MechLayout {
   int32_t NJS, NJE, NWS, NWE;
   int32_t off_js_rc, off_js_cnt, off_js_off, off_jse_f, off_jse_nu32;  // Jacobian nonzeros
   int32_t off_ws_sp, off_ws_cnt, off_ws_off, off_wse_r, off_wse_nu;    // net production per species
+  // Sparse-LU shape (m <= kSparseLuMaxSpecies, else -1): per Jacobian slot of the sliced-ELL
+  // program (off_js_rc), the entry of (row, col) in the static-order filled pattern (int16).
+  int32_t off_js_e;
 };
 
 // Device pointers of one mechanism on one device (passed by value to kernels).
@@ -76,6 +80,9 @@ struct MechDev {
   const int32_t* e3_o1d;      // [e3_no1d][7]: reactions 1..3, photolysis reaction, species 1..3
   const double* e3_o1d_par;   // [e3_no1d][6]: A1, C1, A2, C2, A3, C3
   int32_t e3_no1d, M_index;
+  // Static-order sparse LU program (sparse_lu.hpp), or null when the mechanism is too large.
+  const int32_t* lu_prog;
+  SparseLuLayout lu;
 };
 
 // Host-side packed tables, built from a parsed kinetic model.
@@ -84,6 +91,7 @@ struct HostTables {
   std::vector<unsigned char> blob;
   MechLayout Lx{};                 // mixed form (sliced-ELL programs)
   std::vector<unsigned char> blob_x;
+  SparseLuHost slu;                // sparse-LU program (slu.lay.m == 0: none)
   std::vector<int32_t> rate_type, conv_exp, cf_ptr, cf_idx;
   std::vector<double> rate_param;
   std::vector<int32_t> rx_sidx, rx_n;  // stoichiometry by reaction (MechDev::rx_*)

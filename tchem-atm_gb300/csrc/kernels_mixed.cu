@@ -17,8 +17,8 @@ namespace tchem_gb {
   const void* kernel_##PRE##_##MC##_##RPT();
 TCHEM_GB_DECLARE_SHAPE(mixed, 24, 1)
 TCHEM_GB_DECLARE_SHAPE(mixed, 32, 1)
-TCHEM_GB_DECLARE_SHAPE(mixed, 52, 2)
-TCHEM_GB_DECLARE_SHAPE(mixed, 64, 2)
+TCHEM_GB_DECLARE_SHAPE(mixsp, 64, 2)
+TCHEM_GB_DECLARE_SHAPE(mixsp, 128, 4)
 TCHEM_GB_DECLARE_SHAPE(mixgj, 52, 1_g2)
 TCHEM_GB_DECLARE_SHAPE(mixgj, 64, 1_g2)
 TCHEM_GB_DECLARE_SHAPE(mixgj, 128, 1_g4)
@@ -42,42 +42,45 @@ struct Variant {
   bool simplified;  // the form: TCHEM_GB_FORM_MIXED_SIMPLIFIED (else TCHEM_GB_FORM_MIXED)
   bool gj;          // Gauss-Jordan inverse (else LU)
   bool e3;          // E3SM inputs (per-sample rate constants and source terms)
+  bool sp;          // static-order sparse LU (full Newton; needs the mechanism's LU program)
   const void* kernel;
   cudaError_t (*launch)(const AdvanceParams&, int, int, size_t, cudaStream_t);
 };
 
 // Kernel shapes of each form; a mechanism uses the narrowest with MC >= m and 32 G RPT >= m,
 // among those with the requested threads per sample (32 G; 0: any, fewest warps first). The E3SM
-// time advance has its own instantiations (up to 64 species).
+// time advance has its own instantiations (up to 64 species). In the full-Newton form, one warp
+// per sample above 32 species is the static-order sparse LU (needs the mechanism's LU program).
 const Variant* variants(int* n) {
   static const Variant v[] = {
-      {24, 1, 1, 12, false, false, false, kernel_mixed_24_1(), &launch_mixed_24_1},
-      {32, 1, 1, 12, false, false, false, kernel_mixed_32_1(), &launch_mixed_32_1},
-      {52, 2, 1, 8, false, false, false, kernel_mixed_52_2(), &launch_mixed_52_2},
-      {64, 2, 1, 8, false, false, false, kernel_mixed_64_2(), &launch_mixed_64_2},
-      {52, 1, 2, 16, false, true, false, kernel_mixgj_52_1_g2(), &launch_mixgj_52_1_g2},
-      {64, 1, 2, 12, false, true, false, kernel_mixgj_64_1_g2(), &launch_mixgj_64_1_g2},
-      {128, 1, 4, 8, false, true, false, kernel_mixgj_128_1_g4(), &launch_mixgj_128_1_g4},
-      {24, 1, 1, 12, true, true, false, kernel_simpl_24_1(), &launch_simpl_24_1},
-      {32, 1, 1, 12, true, true, false, kernel_simpl_32_1(), &launch_simpl_32_1},
-      {52, 2, 1, 8, true, true, false, kernel_simpl_52_2(), &launch_simpl_52_2},
-      {64, 2, 1, 8, true, true, false, kernel_simpl_64_2(), &launch_simpl_64_2},
-      {52, 1, 2, 16, true, true, false, kernel_simpl_52_1_g2(), &launch_simpl_52_1_g2},
-      {64, 1, 2, 12, true, true, false, kernel_simpl_64_1_g2(), &launch_simpl_64_1_g2},
-      {128, 1, 4, 8, true, true, false, kernel_simpl_128_1_g4(), &launch_simpl_128_1_g4},
-      {64, 2, 1, 8, false, false, true, kernel_e3mixed_64_2(), &launch_e3mixed_64_2},
-      {64, 2, 1, 8, true, true, true, kernel_e3simpl_64_2(), &launch_e3simpl_64_2},
-      {64, 1, 2, 12, true, true, true, kernel_e3simpl_64_1_g2(), &launch_e3simpl_64_1_g2},
+      {24, 1, 1, 12, false, false, false, false, kernel_mixed_24_1(), &launch_mixed_24_1},
+      {32, 1, 1, 12, false, false, false, false, kernel_mixed_32_1(), &launch_mixed_32_1},
+      {64, 2, 1, 16, false, true, false, true, kernel_mixsp_64_2(), &launch_mixsp_64_2},
+      {128, 4, 1, 8, false, true, false, true, kernel_mixsp_128_4(), &launch_mixsp_128_4},
+      {52, 1, 2, 16, false, true, false, false, kernel_mixgj_52_1_g2(), &launch_mixgj_52_1_g2},
+      {64, 1, 2, 12, false, true, false, false, kernel_mixgj_64_1_g2(), &launch_mixgj_64_1_g2},
+      {128, 1, 4, 8, false, true, false, false, kernel_mixgj_128_1_g4(), &launch_mixgj_128_1_g4},
+      {24, 1, 1, 12, true, true, false, false, kernel_simpl_24_1(), &launch_simpl_24_1},
+      {32, 1, 1, 12, true, true, false, false, kernel_simpl_32_1(), &launch_simpl_32_1},
+      {52, 2, 1, 8, true, true, false, false, kernel_simpl_52_2(), &launch_simpl_52_2},
+      {64, 2, 1, 8, true, true, false, false, kernel_simpl_64_2(), &launch_simpl_64_2},
+      {52, 1, 2, 16, true, true, false, false, kernel_simpl_52_1_g2(), &launch_simpl_52_1_g2},
+      {64, 1, 2, 12, true, true, false, false, kernel_simpl_64_1_g2(), &launch_simpl_64_1_g2},
+      {128, 1, 4, 8, true, true, false, false, kernel_simpl_128_1_g4(), &launch_simpl_128_1_g4},
+      {64, 2, 1, 8, false, false, true, false, kernel_e3mixed_64_2(), &launch_e3mixed_64_2},
+      {64, 2, 1, 8, true, true, true, false, kernel_e3simpl_64_2(), &launch_e3simpl_64_2},
+      {64, 1, 2, 12, true, true, true, false, kernel_e3simpl_64_1_g2(), &launch_e3simpl_64_1_g2},
   };
   *n = static_cast<int>(sizeof(v) / sizeof(v[0]));
   return v;
 }
 
-const Variant* pick(const MechLayout& L, bool simplified, int threads_per_sample, bool e3) {
+const Variant* pick(const MechLayout& L, bool simplified, int threads_per_sample, bool e3, int lu_nnz) {
   int nv = 0;
   const Variant* v = variants(&nv);
   for (int i = 0; i < nv; ++i)
     if (v[i].simplified == simplified && v[i].e3 == e3 && v[i].MC >= L.m && 32 * v[i].G * v[i].RPT >= L.m &&
+        (!v[i].sp || (lu_nnz > 0 && L.off_js_e >= 0)) &&
         (threads_per_sample == 0 || threads_per_sample == 32 * v[i].G))
       return &v[i];
   return nullptr;
@@ -86,10 +89,10 @@ const Variant* pick(const MechLayout& L, bool simplified, int threads_per_sample
 }  // namespace
 
 MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch,
-                         bool simplified, bool e3) {
+                         bool simplified, bool e3, int lu_nnz) {
   if (threads_per_sample != 0 && threads_per_sample != 32 && threads_per_sample != 64 && threads_per_sample != 128)
     throw std::domain_error("mixed forms: threads_per_sample must be 0, 32, 64 or 128");
-  const Variant* best = pick(L, simplified, threads_per_sample, e3);
+  const Variant* best = pick(L, simplified, threads_per_sample, e3, lu_nnz);
   if (!best && e3)
     throw std::domain_error("E3SM time advance: the mixed forms have kernel shapes for up to 64 active species "
                             "(32 or 64 threads per sample for the simplified form, 32 for the FP32-LU form); "
@@ -98,9 +101,9 @@ MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_cou
     throw std::domain_error(simplified ? "simplified form: no kernel shape for this mechanism size and threads_per_sample "
                                          "(up to 64 species with 32 or 64 threads, 128 with 128 threads)"
                                        : "full-Newton FP32 form: no kernel shape for this mechanism size and "
-                                         "threads_per_sample (LU up to 64 species with 32 threads; Gauss-Jordan "
+                                         "threads_per_sample (LU up to 128 species with 32 threads; Gauss-Jordan "
                                          "up to 64 species with 64 threads, 128 with 128 threads)");
-  MixedLayout ml = mixed::make_layout(L, best->MC, best->gj, e3);
+  MixedLayout ml = mixed::make_layout(L, best->MC, best->gj, e3, best->sp ? lu_nnz : 0);
   ml.simplified = simplified ? 1 : (best->gj ? 2 : 0);
   const size_t gbytes = ml.warp_bytes;
   const size_t avail = static_cast<size_t>(max_smem_optin) - 16 - L.blob_bytes;
@@ -124,7 +127,8 @@ MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_cou
 
 cudaError_t launch_trbdf2_mixed(const AdvanceParams& P, const MechLayout& L, int grid, int warps_per_block,
                                 size_t smem, int threads_per_sample, cudaStream_t stream) {
-  const Variant* best = pick(L, P.ml.simplified == 1, threads_per_sample, P.keff_in != nullptr);
+  const int lu_nnz = P.mech.lu_prog ? P.mech.lu.nnz : 0;
+  const Variant* best = pick(L, P.ml.simplified == 1, threads_per_sample, P.keff_in != nullptr, lu_nnz);
   if (!best) return cudaErrorInvalidValue;
   return best->launch(P, grid, warps_per_block * 32, smem, stream);
 }

@@ -17,9 +17,10 @@ struct MixedConfig {
   MixedLayout ml{};
 };
 
-// e3: the E3SM instantiations (per-sample rate constants and source terms).
+// e3: the E3SM instantiations (per-sample rate constants and source terms); lu_nnz: entries of
+// the mechanism's static-order sparse LU (0: no program, the sparse-LU shapes are not used).
 MixedConfig mixed_config(const MechLayout& L, int threads_per_sample, int sm_count, int max_smem_optin, int nbatch,
-                         bool simplified, bool e3 = false);
+                         bool simplified, bool e3 = false, int lu_nnz = 0);
 cudaError_t launch_trbdf2_mixed(const AdvanceParams& P, const MechLayout& L, int grid, int warps_per_block,
                                 size_t smem, int threads_per_sample, cudaStream_t stream);
 

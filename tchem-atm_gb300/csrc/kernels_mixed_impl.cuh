@@ -47,7 +47,9 @@ enum Vec { V_FN = 0, V_FG = 1, V_YP = 2, V_ATOL = 3, V_RTOL = 4, V_YGP = 5, kVec
 enum Stat { S_STEPS = 0, S_REJ = 1, S_NFAIL = 2, S_NEWTON = 3, S_LU = 4, S_SOLVE = 5, S_RHS = 6, S_JAC = 7 };
 
 // src_section: a per-group source-term section (the E3SM kernels' per-sample external sources).
-inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified, bool src_section = false) {
+// lu_nnz > 0: the sparse-LU shape (the factors' entries replace the dense staging matrix).
+inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified, bool src_section = false,
+                               int lu_nnz = 0) {
   auto up16 = [](size_t b) { return static_cast<uint32_t>((b + 15) & ~size_t(15)); };
   MixedLayout ml{};
   ml.LDU = ldu_for(MC);
@@ -61,7 +63,9 @@ inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified, boo
   ml.x32 = o; o += up16(sizeof(float) * L.m);
   ml.keff32 = o; o += up16(sizeof(float) * L.R);
   ml.d32 = o; o += up16(sizeof(float) * (L.NF + 1));  // d32[NF] = 0 is the padding target
-  ml.ustage = o; o += up16(sizeof(float) * static_cast<size_t>(L.m) * ml.LDU);
+  ml.ustage = o;
+  if (lu_nnz == 0) o += up16(sizeof(float) * static_cast<size_t>(L.m) * ml.LDU);
+  ml.lu = o; o += up16(sizeof(float) * static_cast<size_t>(lu_nnz));
   ml.lrow = o;  // L factor by row (LU forms only)
   if (!simplified) o += up16(sizeof(float) * static_cast<size_t>(L.m) * ml.LDL);
   ml.pinv = o; o += up16(sizeof(float) * L.m);
@@ -92,9 +96,16 @@ inline MixedLayout make_layout(const MechLayout& L, int MC, bool simplified, boo
 // (a new matrix every jacobian_interval iterations, the reference's stage guesses and 2-norm
 // test) with one FP64-residual refinement sweep per solve, like the FP32-LU form: it follows the
 // FP64 Newton iterates with matrix-vector solves instead of triangular ones.
-template <int MC, int RPT, bool SIMP, int G = 1, bool FULLGJ = false, bool E3 = false>
+//
+// SP (with FULLGJ, one warp) replaces the dense linear algebra by the static-order sparse LU
+// (sparse_lu.hpp): the Newton matrix is assembled into the filled pattern's entries in shared
+// memory, factored without pivot search by the mechanism's update program (one __syncwarp per
+// elimination step) and applied by column-oriented substitutions; full Newton and the refinement
+// sweep are unchanged. MC is then only the width of the solve vector (>= m).
+template <int MC, int RPT, bool SIMP, int G = 1, bool FULLGJ = false, bool E3 = false, bool SP = false>
 struct Solver {
   static_assert(!FULLGJ || SIMP, "the full-Newton Gauss-Jordan variant uses the inverse");
+  static_assert(!SP || (FULLGJ && G == 1 && !E3), "the sparse-LU shape is a one-warp full-Newton shape");
   static constexpr bool kSimplifiedNewton = SIMP && !FULLGJ;
   static_assert(MC % 4 == 0, "MC must be a multiple of 4");
   static_assert(G == 1 || RPT == 1, "multi-warp samples: one row per thread");
@@ -714,6 +725,166 @@ struct Solver {
     count(S_SOLVE);
   }
 
+  // ---- static-order sparse LU (SP) --------------------------------------------------------
+  __device__ __forceinline__ const int32_t* lp(int32_t off) const { return P.mech.lu_prog + off; }
+
+  // A = I - coef J(y) (FP32) into the filled pattern's entries: zero, unit diagonal, then the
+  // Jacobian nonzeros through the sliced-ELL program (each slot's entry from the js_e table).
+  __device__ __forceinline__ void newton_matrix_sp(const double (&y)[RPT], double coef) {
+    const MechLayout& L = P.mech.L;
+    const int mm = L.m;
+    float* x32 = w<float>(P.ml.x32);
+    float* d32 = w<float>(P.ml.d32);
+    float* lu = w<float>(P.ml.lu);
+    const float* keff32 = w<float>(P.ml.keff32);
+    const int nz4 = (P.mech.lu.nnz + 3) >> 2;
+#pragma unroll
+    for (int s = 0; s < RPT; ++s)
+      if (row(s) < mm) x32[row(s)] = static_cast<float>(y[s]);
+    for (int e = lane; e < nz4; e += 32) reinterpret_cast<float4*>(lu)[e] = make_float4(0.f, 0.f, 0.f, 0.f);
+    __syncwarp();
+    const int32_t* diag = lp(P.mech.lu.off_diag);
+    for (int k = lane; k < mm; k += 32) lu[__ldg(diag + k)] = 1.f;
+    const int32_t* rf_ptr = t<int32_t>(L.off_rf_ptr);
+    const int16_t* rf_sp = t<int16_t>(L.off_rf_sp);
+#pragma unroll 2
+    for (int r = lane; r < L.R; r += 32) {
+      const int f0 = rf_ptr[r], f1 = rf_ptr[r + 1];
+      const float kr = keff32[r];
+      if (f1 - f0 == 1) {
+        d32[f0] = kr;
+      } else if (f1 - f0 == 2) {
+        const float xa = x32[rf_sp[f0]], xb = x32[rf_sp[f0 + 1]];
+        d32[f0] = kr * xb;
+        d32[f0 + 1] = kr * xa;
+      } else {
+        for (int f = f0; f < f1; ++f) {
+          float dv = kr;
+          for (int g = f0; g < f1; ++g)
+            if (g != f) dv *= x32[rf_sp[g]];
+          d32[f] = dv;
+        }
+      }
+    }
+    __syncwarp();
+    const float c = static_cast<float>(coef);
+    const int32_t* js_rc = t<int32_t>(L.off_js_rc);
+    const int16_t* js_e = t<int16_t>(L.off_js_e);
+    const int32_t* js_cnt = t<int32_t>(L.off_js_cnt);
+    const int32_t* js_off = t<int32_t>(L.off_js_off);
+    const int16_t* jse_f = t<int16_t>(L.off_jse_f);
+    const float* jse_nu = t<float>(L.off_jse_nu32);
+#pragma unroll 2
+    for (int sl = 0; sl < L.NJS; ++sl) {
+      const int rc = js_rc[sl * 32 + lane];
+      const int cnt = js_cnt[sl];
+      const int base = js_off[sl] + lane;
+      float J0 = 0.f, J1 = 0.f;
+      int cc = 0;
+      for (; cc + 2 <= cnt; cc += 2) {
+        const int e = base + 32 * cc;
+        const int f0 = jse_f[e], f1 = jse_f[e + 32];
+        J0 += jse_nu[e] * d32[f0];
+        J1 += jse_nu[e + 32] * d32[f1];
+      }
+      if (cc < cnt) J0 += jse_nu[base + 32 * cc] * d32[jse_f[base + 32 * cc]];
+      if (rc >= 0) {
+        const int i = rc >> 16, j = rc & 0xffff;
+        lu[js_e[sl * 32 + lane]] = (i == j ? 1.f : 0.f) - c * (J0 + J1);
+      }
+    }
+    __syncwarp();
+    count(S_JAC);
+  }
+
+  // In-place factorization P A P^T = L U in the static order: per step k the pivot's reciprocal
+  // (kept in pinv for the back substitution), the column of L scaled by it, then the step's
+  // trailing updates, lane-strided over the program's lists. Returns false on a zero or
+  // non-finite pivot (the same for every lane: the pivot is one shared-memory word).
+  __device__ __forceinline__ bool factor_sp() {
+    const int mm = m();
+    float* lu = w<float>(P.ml.lu);
+    float* dinv = w<float>(P.ml.pinv);
+    const SparseLuLayout& S = P.mech.lu;
+    const int32_t* diag = lp(S.off_diag);
+    const int32_t* lcp = lp(S.off_lc_ptr);
+    const int32_t* lc = lp(S.off_lc);
+    const int32_t* upp = lp(S.off_up_ptr);
+    const int2* up = reinterpret_cast<const int2*>(lp(S.off_up));
+#pragma unroll 1
+    for (int k = 0; k < mm; ++k) {
+      const float piv = lu[__ldg(diag + k)];
+      if (!(fabsf(piv) > 0.f) || !(fabsf(piv) < INFINITY)) return false;
+      const float rinv = __frcp_rn(piv);
+      if (lane == 0) dinv[k] = rinv;
+      const int a1 = __ldg(lcp + k + 1);
+      for (int q = __ldg(lcp + k) + lane; q < a1; q += 32) {
+        const int e = __ldg(lc + q) & 0xffff;
+        lu[e] *= rinv;
+      }
+      __syncwarp();
+      const int b1 = __ldg(upp + k + 1);
+      for (int q = __ldg(upp + k) + lane; q < b1; q += 32) {
+        const int2 op = __ldg(up + q);
+        const int dst = op.x & 0xffff, l = static_cast<int>(static_cast<uint32_t>(op.x) >> 16);
+        lu[dst] = fmaf(-lu[l], lu[op.y], lu[dst]);
+      }
+      __syncwarp();
+    }
+    count(S_LU);
+    return true;
+  }
+
+  // x = A^{-1} g with the sparse factors (g, x by row): g scattered to position order in ybuf,
+  // forward substitution by columns of L, back substitution by columns of U (x_k = z_k / u_kk).
+  __device__ __forceinline__ void solve_sp(const float (&gf)[RPT], double (&x)[RPT]) {
+    const int mm = m();
+    const float* lu = w<float>(P.ml.lu);
+    const float* dinv = w<float>(P.ml.pinv);
+    float* wv = w<float>(P.ml.ybuf);
+    const SparseLuLayout& S = P.mech.lu;
+    const int32_t* pos = lp(S.off_pos);
+    const int32_t* lcp = lp(S.off_lc_ptr);
+    const int32_t* lc = lp(S.off_lc);
+    const int32_t* ucp = lp(S.off_uc_ptr);
+    const int32_t* uc = lp(S.off_uc);
+    int ps[RPT];
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) {
+      ps[s] = row(s) < mm ? __ldg(pos + row(s)) : 0;
+      if (row(s) < mm) wv[ps[s]] = gf[s];
+    }
+    __syncwarp();
+#pragma unroll 1
+    for (int k = 0; k < mm; ++k) {
+      const float zk = wv[k];
+      const int a1 = __ldg(lcp + k + 1);
+      for (int q = __ldg(lcp + k) + lane; q < a1; q += 32) {
+        const int v = __ldg(lc + q);
+        const int i = static_cast<int>(static_cast<uint32_t>(v) >> 16);
+        wv[i] = fmaf(-lu[v & 0xffff], zk, wv[i]);
+      }
+      __syncwarp();
+    }
+#pragma unroll 1
+    for (int k = mm - 1; k >= 0; --k) {
+      const float xk = wv[k] * dinv[k];
+      const int a1 = __ldg(ucp + k + 1);
+      for (int q = __ldg(ucp + k) + lane; q < a1; q += 32) {
+        const int v = __ldg(uc + q);
+        const int i = static_cast<int>(static_cast<uint32_t>(v) >> 16);
+        wv[i] = fmaf(-lu[v & 0xffff], xk, wv[i]);
+      }
+      __syncwarp();
+      if (lane == 0) wv[k] = xk;  // after every lane has read z_k
+    }
+    __syncwarp();
+#pragma unroll
+    for (int s = 0; s < RPT; ++s) x[s] = row(s) < mm ? static_cast<double>(wv[ps[s]]) : 0.0;
+    __syncwarp();
+    count(S_SOLVE);
+  }
+
   // Forward substitution with the stored multipliers (rows' values in wf, in place); leaves the
   // values in step order in ybuf.
   __device__ __forceinline__ void forward(float (&wf)[RPT]) {
@@ -896,6 +1067,15 @@ struct Solver {
     return false;
   }
 
+  // x = A^{-1} g with the current FP32 factors: the Gauss-Jordan inverse or the sparse LU.
+  __device__ __forceinline__ void lin_solve(const float (&gf)[RPT], double (&x)[RPT]) {
+    if constexpr (SP) {
+      solve_sp(gf, x);
+    } else {
+      apply_inverse(gf, x);
+    }
+  }
+
   // ---- full Newton with the Gauss-Jordan inverse and one refinement sweep per solve --------
   __device__ __forceinline__ bool newton_full_gj(double (&y)[RPT], const double (&rv)[RPT], double coef,
                                                  int max_newton, int jac_interval, double atol, double rtol) {
@@ -909,16 +1089,21 @@ struct Solver {
         wf[s] = static_cast<float>(g[s]);
       }
       if (it % jac_interval == 0) {
-        newton_matrix(y, coef);
-        put(V_YGP, y);  // the point of the inverted Jacobian, for the refinement residual
-        if (!invert()) return false;
+        put(V_YGP, y);  // the point of the factored Jacobian, for the refinement residual
+        if constexpr (SP) {
+          newton_matrix_sp(y, coef);
+          if (!factor_sp()) return false;
+        } else {
+          newton_matrix(y, coef);
+          if (!invert()) return false;
+        }
       }
-      apply_inverse(wf, dx);
-      // refinement: FP64 residual of (I - c J) dx = g, correction through the FP32 inverse
+      lin_solve(wf, dx);
+      // refinement: FP64 residual of (I - c J) dx = g, correction through the FP32 factors
       jvec(dx, jd);
 #pragma unroll
       for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(g[s] - (dx[s] - coef * jd[s]));
-      apply_inverse(wf, corr);
+      lin_solve(wf, corr);
       count(S_NEWTON);
       double sdx = 0.0, sy = 0.0;
 #pragma unroll
@@ -1049,8 +1234,8 @@ struct Solver {
 #pragma unroll
         for (int s = 0; s < RPT; ++s) wf[s] = static_cast<float>(est[s]);
         if constexpr (FULLGJ) {
-          // filter with the last Newton iteration's inverse (the reference's matrix)
-          apply_inverse(wf, estf);
+          // filter with the last Newton iteration's factors (the reference's matrix)
+          lin_solve(wf, estf);
         } else if constexpr (SIMP) {
           // filter with I - c J(y_{n+1}); the inverse is carried into the next step
           newton_matrix(y1, d * dt);
@@ -1116,14 +1301,16 @@ struct Solver {
 // the plain kernel).
 // Shapes with one row per thread hold half the matrix registers of the two-rows-per-lane shapes,
 // so they fit 168 registers and run 12 warps per SM (the 52-column two-warp shape 128 registers
-// and 16 warps); the others run 8.
-template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false, bool E3 = false>
+// and 16 warps); the others run 8. The sparse-LU shapes hold no matrix registers: 16 warps for up
+// to 64 species (shared memory then limits the samples per CTA), 8 for up to 128.
+template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false, bool E3 = false, bool SP = false>
 constexpr int max_threads() {
+  if (SP) return RPT <= 2 ? 512 : 256;
   return (RPT == 1 && MC <= 52 && G == 2) ? 512 : ((RPT == 1 && MC <= 64) ? 384 : 256);
 }
 
-template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false, bool E3 = false>
-__global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G, FULLGJ, E3>(), 1)
+template <int MC, int RPT, bool SIMP, int G, bool FULLGJ = false, bool E3 = false, bool SP = false>
+__global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G, FULLGJ, E3, SP>(), 1)
     trbdf2_mixed_kernel(const __grid_constant__ AdvanceParams P) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
@@ -1135,7 +1322,7 @@ __global__ void __launch_bounds__(max_threads<MC, RPT, SIMP, G, FULLGJ, E3>(), 1
   }
   constexpr int NT = 32 * G;
   const int group = threadIdx.x / NT, tid = threadIdx.x % NT, lane = threadIdx.x & 31;
-  Solver<MC, RPT, SIMP, G, FULLGJ, E3> S{P, tables, tables + L.blob_bytes + group * P.ml.warp_bytes, lane, tid, tid >> 5,
+  Solver<MC, RPT, SIMP, G, FULLGJ, E3, SP> S{P, tables, tables + L.blob_bytes + group * P.ml.warp_bytes, lane, tid, tid >> 5,
                              1 + group};
   const int m = L.m;
   const int n_items = P.n_items_dev ? *P.n_items_dev : P.n_items;

@@ -101,6 +101,7 @@ def lib() -> C.CDLL:
         "tchem_gb_mech_destroy": (None, [vp]),
         "tchem_gb_mech_host_view": (C.c_int, [vp, C.POINTER(KmcdView)]),
         "tchem_gb_mech_species_name": (C.c_int, [vp, C.c_int, C.c_char_p, C.c_int]),
+        "tchem_gb_mech_sparse_lu": (C.c_int, [vp, vp, vp, C.c_int]),
         "tchem_gb_scenario_batch_size": (C.c_int, [C.c_char_p, C.POINTER(C.c_int)]),
         "tchem_gb_scenario_read": (C.c_int, [C.c_char_p, vp, vp, C.c_int]),
         "tchem_gb_mech_e3sm_view": (C.c_int, [vp, C.POINTER(E3smView)]),
