@@ -225,8 +225,10 @@ int tchem_gb_aero_scenario_particles(const char* yaml_path, const tchem_gb_aero*
 /* Numerical form of the time advance. */
 enum tchem_gb_form {
   TCHEM_GB_FORM_PLAIN_FP64 = 0, /* FP64 Newton LU: the parity form */
-  /* The reference's full Newton with FP32 linear algebra -- an LU (one warp per sample) or a
-     Gauss-Jordan inverse (two warps per sample, threads_per_sample = 64) -- and one sweep of
+  /* The reference's full Newton with FP32 linear algebra -- an LU (one warp per sample,
+     threads_per_sample = 32: dense with partial pivoting up to 32 species, the static-order sparse
+     LU of tchem_gb_mech_sparse_lu from 33 to 128) or a Gauss-Jordan inverse (two or four warps per
+     sample, threads_per_sample = 64 or 128) -- and one sweep of
      iterative refinement per Newton solve (FP64 residual of the linear system with the FP64
      Jacobian, FP32 correction); FP64 Newton residual, state and error control: follows the FP64
      form's Newton iterates. */

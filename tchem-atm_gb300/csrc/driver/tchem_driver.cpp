@@ -68,6 +68,8 @@ struct Driver {
     ws_bytes = tchem_gb_aero_workspace_bytes(mech, aero, nBatch);
     if (ws_bytes == 0) check(TCHEM_GB_ERR_ARG, "tchem_gb_aero_workspace_bytes");
     check_cuda(cudaMalloc(&d_ws, ws_bytes), "cudaMalloc(workspace)");
+    // the workspace header (work queue, device error word) starts zeroed, as the C ABI requires
+    check_cuda(cudaMemset(d_ws, 0, ws_bytes), "cudaMemset(workspace)");
     const double tol_newton[2] = {num.atol_newton, num.rtol_newton};
     std::vector<double> tol_time(2 * static_cast<size_t>(n_ode));
     for (int i = 0; i < n_ode; ++i) {
