@@ -215,7 +215,7 @@ int tchem_gb_mech_sparse_lu(const tchem_gb_mech* mech, int32_t* info, int32_t* p
   }
   const tchem_gb::SparseLuHost& h = mm->host_tables->slu;
   if (h.lay.m == 0) {
-    set_last_error("tchem_gb_mech_sparse_lu: no sparse LU program (more than 128 active species)");
+    set_last_error("tchem_gb_mech_sparse_lu: no sparse LU program for this mechanism (more than 128 active species)");
     return TCHEM_GB_ERR_UNSUPPORTED;
   }
   const tchem_gb::SparseLuLayout& L = h.lay;

@@ -317,12 +317,17 @@ HostTables build_host_tables(const KineticModel& km) {
     if (m <= kSparseLuMaxSpecies) {
       std::vector<std::pair<int, int>> nz;
       for (const auto& kv : jac) nz.push_back(kv.first);
-      ht.slu = build_sparse_lu(m, nz);
-      for (int32_t rc : js.item) {
-        int e = 0;
-        if (rc >= 0) e = ht.slu.entry[static_cast<size_t>(ht.slu.pos[rc >> 16]) * m + ht.slu.pos[rc & 0xffff]];
-        js_e.push_back(static_cast<int16_t>(e));
+      try {
+        ht.slu = build_sparse_lu(m, nz);
+      } catch (const std::exception&) {
+        ht.slu = SparseLuHost{};  // no program: the sparse-LU shapes are not offered
       }
+      if (ht.slu.lay.m == m)
+        for (int32_t rc : js.item) {
+          int e = 0;
+          if (rc >= 0) e = ht.slu.entry[static_cast<size_t>(ht.slu.pos[rc >> 16]) * m + ht.slu.pos[rc & 0xffff]];
+          js_e.push_back(static_cast<int16_t>(e));
+        }
     }
     const Sliced ws = make_slices(per_species, wids, static_cast<int16_t>(R));
     std::vector<float> jse_nu32(js.val.begin(), js.val.end());

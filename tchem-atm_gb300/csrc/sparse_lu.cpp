@@ -54,7 +54,8 @@ SparseLuHost build_sparse_lu(int m, const std::vector<std::pair<int, int>>& nonz
   for (int k = 0; k < m; ++k)
     for (int l = 0; l < m; ++l)
       if (F(k, l)) h.entry[static_cast<size_t>(k) * m + l] = nnz++;
-  if (nnz > 0xffff) throw std::invalid_argument("sparse LU: too many entries for the program encoding");
+  // entries travel as 16-bit fields (signed in the sliced-ELL slot table)
+  if (nnz > 0x7fff) throw std::invalid_argument("sparse LU: too many entries for the program encoding");
   auto E = [&](int k, int l) { return h.entry[static_cast<size_t>(k) * m + l]; };
 
   SparseLuLayout& L = h.lay;
