@@ -263,6 +263,13 @@ int g_lu_tile_bits = 0;
 // structural nonzeros (the skipped ones only ever add 0 to 0).
 std::vector<int> g_lu_order;
 
+// Test settings of the full-Newton integrator (oracle_set_newton_min_iterations,
+// oracle_set_step_doubling): a minimum number of Newton iterations per stage before the
+// convergence test may end it, and a step sequence imposed as pure doubling (every step accepted,
+// the next one twice as long, the last one clipped to t_end) in place of the error control.
+int g_newton_min_iters = 1;
+bool g_step_doubling = false;
+
 // Round-to-nearest-even of an FP32 value to `keep` mantissa bits (TF32: 10, BF16: 7).
 float round_mantissa(float x, int keep) {
   uint32_t u;
@@ -621,7 +628,7 @@ struct Sample {
       }
       const double ndx = std::sqrt(sdx), ny = std::sqrt(sy);
       if (!std::isfinite(ndx) || !std::isfinite(ny)) return false;
-      if (ndx <= s.atol_newton + s.rtol_newton * ny) return true;
+      if (it + 1 >= g_newton_min_iters && ndx <= s.atol_newton + s.rtol_newton * ny) return true;
     }
     return false;
   }
@@ -706,6 +713,7 @@ struct Sample {
         err = std::max(err, std::abs(estf[i]) / w);
       }
       if (!std::isfinite(err)) { status = TCHEM_GB_SAMPLE_NONFINITE; break; }
+      if (g_step_doubling) err = 0.0;  // factor 2 below
       if (err <= 1.0 || dt <= dt_min) {
         if (tape_dt) {
           if (st.n_steps >= tape_cap) { status = TCHEM_GB_SAMPLE_TAPE_FULL; break; }
@@ -966,6 +974,17 @@ int oracle_set_lu_tile_bits(int bits) {
 }
 
 // Static elimination order of FP32 factorizations of n x n matrices (n = 0: partial pivoting).
+int oracle_set_newton_min_iterations(int k) {
+  if (k < 1 || k > 20) return TCHEM_GB_ERR_ARG;
+  g_newton_min_iters = k;
+  return TCHEM_GB_OK;
+}
+
+int oracle_set_step_doubling(int on) {
+  g_step_doubling = on != 0;
+  return TCHEM_GB_OK;
+}
+
 int oracle_set_lu_static_order(int n, const int32_t* order) {
   if (n < 0 || (n > 0 && !order)) return TCHEM_GB_ERR_ARG;
   std::vector<int> o(order, order + n), seen(n, 0);

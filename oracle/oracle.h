@@ -22,7 +22,10 @@
  *                    failure halves dt up to 4 times, then the sample fails with state 0,
  *                    t_out = t_end, dt_out = -1 (src/core/impl/TChem_Impl_TimeIntegratorImplicitEuler.hpp:246-305).
  * The Jacobian is analytic (the reference uses forward differences or Sacado AD; both give
- * the same matrix to rounding, and the Newton fixed point does not depend on it).
+ * the same matrix to rounding, and the Newton fixed point does not depend on it). Newton stops when
+ * ||dx|| <= atol + rtol ||y|| (2-norms); where a few huge entries dominate ||y|| (the aerosol number
+ * concentrations of the E3SM uci_col scenario) that ends most stages after one iteration, so the
+ * end state then depends on the stage guesses (oracle_set_newton_min_iterations makes it iterate).
  */
 #ifndef TCHEM_GB_ORACLE_H
 #define TCHEM_GB_ORACLE_H
@@ -41,6 +44,12 @@ int oracle_set_lu_tile_bits(int bits);
  * sparse factorization computes them: row and column k are species order[k]; the substitutions are
  * column-oriented with the pivots' reciprocals. n = 0 restores partial pivoting. Process-wide. */
 int oracle_set_lu_static_order(int n, const int32_t* order);
+/* Full-Newton integrator test settings (process-wide): at least k Newton iterations per stage
+ * before the convergence test may end it (1: the default), and a step sequence imposed as pure
+ * doubling (on != 0: every step accepted and the next one twice as long, the last clipped to t_end;
+ * the error estimate is not used). */
+int oracle_set_newton_min_iterations(int k);
+int oracle_set_step_doubling(int on);
 /* One FP32 matrix a[n][n] factored as the tensor-core LU does: 32-column panels with partial
  * pivoting, trailing update on operands rounded to `keep` mantissa bits (10: TF32, 23: none);
  * lu[n][n] and piv[n] as LAPACK's sgetrf (0-based pivots). */
