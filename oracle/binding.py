@@ -22,8 +22,8 @@ def load(native: bool = False) -> C.CDLL:
         L.oracle_set_lu_tile_bits.argtypes = [C.c_int]
         L.oracle_set_newton_min_iterations.restype = C.c_int
         L.oracle_set_newton_min_iterations.argtypes = [C.c_int]
-        L.oracle_set_step_doubling.restype = C.c_int
-        L.oracle_set_step_doubling.argtypes = [C.c_int]
+        L.oracle_set_step_sequence.restype = C.c_int
+        L.oracle_set_step_sequence.argtypes = [C.c_int, C.c_void_p]
         L.oracle_set_lu_static_order.restype = C.c_int
         L.oracle_set_lu_static_order.argtypes = [C.c_int, C.c_void_p]
         L.oracle_lu_factor_blocked.restype = C.c_int

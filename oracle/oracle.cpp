@@ -264,11 +264,12 @@ int g_lu_tile_bits = 0;
 std::vector<int> g_lu_order;
 
 // Test settings of the full-Newton integrator (oracle_set_newton_min_iterations,
-// oracle_set_step_doubling): a minimum number of Newton iterations per stage before the
-// convergence test may end it, and a step sequence imposed as pure doubling (every step accepted,
-// the next one twice as long, the last one clipped to t_end) in place of the error control.
+// oracle_set_step_sequence): a minimum number of Newton iterations per stage before the
+// convergence test may end it, and an imposed sequence of accepted step sizes (step k takes
+// g_step_seq[k], the last entry repeating, each clipped to t_end as usual) in place of the error
+// control.
 int g_newton_min_iters = 1;
-bool g_step_doubling = false;
+std::vector<double> g_step_seq;
 
 // Round-to-nearest-even of an FP32 value to `keep` mantissa bits (TF32: 10, BF16: 7).
 float round_mantissa(float x, int keep) {
@@ -653,6 +654,8 @@ struct Sample {
     for (int iter = 0; iter < s.max_iters && t < t_end; ++iter) {
       bool converged = false, last = false;
       for (int ntry = 0; ntry < 4; ++ntry) {
+        if (!g_step_seq.empty() && ntry == 0)
+          dt = g_step_seq[std::min<size_t>(static_cast<size_t>(st.n_steps), g_step_seq.size() - 1)];
         dt = std::min(std::max(dt, dt_min), dt_max);
         last = dt >= t_end - t;
         if (last) dt = t_end - t;
@@ -713,7 +716,7 @@ struct Sample {
         err = std::max(err, std::abs(estf[i]) / w);
       }
       if (!std::isfinite(err)) { status = TCHEM_GB_SAMPLE_NONFINITE; break; }
-      if (g_step_doubling) err = 0.0;  // factor 2 below
+      if (!g_step_seq.empty()) err = 0.0;  // the imposed step is accepted
       if (err <= 1.0 || dt <= dt_min) {
         if (tape_dt) {
           if (st.n_steps >= tape_cap) { status = TCHEM_GB_SAMPLE_TAPE_FULL; break; }
@@ -980,8 +983,11 @@ int oracle_set_newton_min_iterations(int k) {
   return TCHEM_GB_OK;
 }
 
-int oracle_set_step_doubling(int on) {
-  g_step_doubling = on != 0;
+int oracle_set_step_sequence(int n, const double* dt) {
+  if (n < 0 || (n > 0 && !dt)) return TCHEM_GB_ERR_ARG;
+  for (int k = 0; k < n; ++k)
+    if (!(dt[k] > 0.0)) return TCHEM_GB_ERR_ARG;
+  g_step_seq.assign(dt, dt + n);
   return TCHEM_GB_OK;
 }
 

@@ -45,11 +45,11 @@ int oracle_set_lu_tile_bits(int bits);
  * column-oriented with the pivots' reciprocals. n = 0 restores partial pivoting. Process-wide. */
 int oracle_set_lu_static_order(int n, const int32_t* order);
 /* Full-Newton integrator test settings (process-wide): at least k Newton iterations per stage
- * before the convergence test may end it (1: the default), and a step sequence imposed as pure
- * doubling (on != 0: every step accepted and the next one twice as long, the last clipped to t_end;
- * the error estimate is not used). */
+ * before the convergence test may end it (1: the default), and an imposed sequence of accepted step
+ * sizes dt[n] (step k takes dt[min(k, n - 1)], clipped to t_end as usual; the error estimate is not
+ * used; n = 0 restores the error control). A Newton failure still halves the step. */
 int oracle_set_newton_min_iterations(int k);
-int oracle_set_step_doubling(int on);
+int oracle_set_step_sequence(int n, const double* dt);
 /* One FP32 matrix a[n][n] factored as the tensor-core LU does: 32-column panels with partial
  * pivoting, trailing update on operands rounded to `keep` mantissa bits (10: TF32, 23: none);
  * lu[n][n] and piv[n] as LAPACK's sgetrf (0-based pivots). */

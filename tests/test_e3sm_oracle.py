@@ -136,17 +136,17 @@ def test_uci_col_time_advance_matches_reference():
     assert tolerance_units(out[:, 3:3 + m], golden[:, 6:6 + m], s["atol_time"], s["rtol_time"]).max() <= 10.0
 
 
-def test_uci_col_reference_step_sequence_reproduces_72_columns_to_1e8():
+def test_uci_col_reference_step_sequence_reproduces_every_column_to_1e8():
     """Where the reference's output pins its step sequence, its arithmetic is reproduced to the
     reference's own 1e-8 file criterion. The golden's dt_out (577.685 in columns 8-79, 388.791 in
-    0-7) is 2 x the clipped last step of pure doubling from dt_in = 1e-20 (78 steps), with one
-    halving near 189 s in columns 0-7. Two facts of the reference run follow. Its Newton stages are
-    converged: the restatement's 2-norm test (tol_newton relative to ||y||) ends nearly every stage
-    after one iteration here, because the aerosol number concentrations (up to 1.3e11) dominate ||y||,
-    and that result is 1e-6 from the golden, while iterating to convergence brings columns 8-79
-    to 2e-11 of it. Its step controller doubles at every step of those columns, where the
-    restatement's error control (Hosea & Shampine's filtered estimate) takes 79-86 steps; that
-    controller is inside Tines, which is absent, so columns 0-7 are not pinned."""
+    0-7) is 2 x the clipped last step of pure doubling from dt_in = 1e-20, in columns 0-7 with the
+    step tried at 189 s halved once. Imposing those accepted steps and iterating Newton to
+    convergence reproduces every column to about 1e-11. Two facts of the reference run follow. Its
+    Newton stages are converged: the restatement's 2-norm test (tol_newton relative to ||y||) ends
+    nearly every stage after one iteration on this state, because the aerosol number
+    concentrations (up to 1.3e11) dominate ||y||, and that result is 1e-6 from the golden. And its
+    step controller is not the restatement's (Hosea & Shampine's filtered estimate takes 79-86
+    steps here): that controller is inside Tines, which is absent."""
     s = manifest()["e3sm"]["uci_col_full_gas.npy"]["settings"]
     km, state, photo, ext = uci_col()
     B, m = state.shape[0], km.n_active
@@ -160,15 +160,27 @@ def test_uci_col_reference_step_sequence_reproduces_72_columns_to_1e8():
     stages = 2 * (stats["n_steps"] + stats["n_rejected"])
     assert stats["n_newton_iter"].sum() <= 1.05 * stages.sum()
     assert np.mean(stats["n_newton_iter"] == stages) >= 0.8
-    assert L.oracle_set_newton_min_iterations(3) == 0 and L.oracle_set_step_doubling(1) == 0
-    try:
-        out, t, dt, status, stats = o.time_advance(uci_col_tadv(B, s), state, photo, ext, tn, tol_time)
-    finally:
-        L.oracle_set_newton_min_iterations(1)
-        L.oracle_set_step_doubling(0)
-    assert np.all(status == 0) and np.all(t == 1800.0) and np.all(stats["n_steps"] == 78)
-    assert compare_files_values(printed(out[8:, 3:]), golden[8:, 6:]) <= 1e-8
+    doubling = s["dt_in"] * 2.0 ** np.arange(78)               # columns 8-79
+    halved = np.concatenate([doubling[:74], doubling[73:78]])  # columns 0-7: 189 s step halved
+    for seq, cols, dt_out in ((doubling, slice(8, 80), 577.685), (halved, slice(0, 8), 388.791)):
+        # the reference's dt_out: twice the last step, clipped to t_end
+        assert abs(2.0 * (s["tend"] - seq[:-1].sum()) - dt_out) < 1e-3
+        assert np.allclose(golden[cols, 2], dt_out, atol=1e-3)
+        sel = np.arange(B)[cols]
+        seq = np.ascontiguousarray(seq)
+        assert L.oracle_set_newton_min_iterations(3) == 0
+        assert L.oracle_set_step_sequence(len(seq), seq.ctypes.data) == 0
+        try:
+            out, t, dt, status, st = o.time_advance(uci_col_tadv(len(sel), s), state[sel], photo[sel], ext[sel], tn,
+                                                    tol_time)
+        finally:
+            L.oracle_set_newton_min_iterations(1)
+            L.oracle_set_step_sequence(0, None)
+        assert np.all(status == 0) and np.all(t == 1800.0) and np.all(st["n_steps"] == len(seq))
+        assert compare_files_values(printed(out[:, 3:]), golden[cols, 6:]) <= 1e-8
     assert L.oracle_set_newton_min_iterations(0) != 0
+    bad = np.array([1.0, -1.0])
+    assert L.oracle_set_step_sequence(2, bad.ctypes.data) != 0
 
 
 def test_state_dependent_rate_constants_are_rejected():
