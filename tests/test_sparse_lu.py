@@ -185,3 +185,55 @@ def test_oracle_static_order_time_advance_within_1e7_of_fp64(mechs):
     assert err.max() <= 1e-7
     bad = np.array([0, 0, 5], dtype=np.int32)
     assert L.oracle_set_lu_static_order(3, bad.ctypes.data) != 0
+
+
+TINY = """NCAR-version: v1.0
+constant_species:
+- name: M
+species:
+- name: A
+- name: B
+- name: C
+reactions:{reactions}
+"""
+
+R_AB = """
+- type: ARRHENIUS
+  reactants:
+    A: 1
+  products:
+    B: 1
+  coefficients:
+    A: 0.5"""
+R_CYCLE = """
+- type: ARRHENIUS
+  reactants:
+    A: 1
+    B: 1
+  products:
+    C: 2
+  coefficients:
+    A: 1.0e-3
+- type: ARRHENIUS
+  reactants:
+    C: 1
+  products:
+    A: 1
+  coefficients:
+    A: 2.0"""
+
+
+@pytest.mark.parametrize("reactions,nnz", [(" []", 3), (R_AB, 4), (R_CYCLE, None)])
+def test_small_mechanisms(reactions, nnz):
+    """Edge cases of the program builder: a mechanism without reactions (the identity), one
+    first-order reaction, and a cycle; each solved exactly in FP64."""
+    km = KineticModel.from_string(TINY.format(reactions=reactions))
+    P = program(km)
+    assert P["m"] == 3
+    if nnz is not None:
+        assert P["nnz"] == nnz
+    A, _ = newton_matrix(km, 2, 10.0)
+    a = assemble(P, A, np.float64)
+    dinv = factor(P, a)
+    g = np.array([1.0, -2.0, 0.5])
+    np.testing.assert_allclose(solve(P, a, dinv, g), np.linalg.solve(A, g), rtol=1e-12, atol=1e-15)
